@@ -1,0 +1,352 @@
+"""CPU oracle for the cc3d labelling path.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.
+
+Two interchangeable cores sit under one Python front end that restates the
+reference's Cython layer (cc3d/fastcc3d.pyx):
+
+* ``"port"``      -- oracle/cc3d_oracle.c, a plain C restatement of the
+                     labelling contract (always available; built by make).
+* ``"reference"`` -- oracle/_ref/libcc3d_ref.so, the reference's own C++
+                     headers compiled from its source tree by oracle/Makefile
+                     (only where that tree exists).
+
+Statistics are restated in numpy (cc3d/fastcc3d.pyx:681-938).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from functools import reduce
+import operator
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libcc3d_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libcc3d_ref.so")
+
+DT_CODES = {
+    np.dtype(np.uint8): 1, np.dtype(np.uint16): 2, np.dtype(np.uint32): 3,
+    np.dtype(np.uint64): 4, np.dtype(np.float32): 5, np.dtype(np.float64): 6,
+}
+
+
+class DimensionError(Exception):
+    """The array has the wrong number of dimensions (cc3d/fastcc3d.pyx:123-125)."""
+
+
+def build(quiet: bool = True) -> None:
+    """Compile the oracle (and the reference shim when its sources exist)."""
+    kw = dict(stdout=subprocess.DEVNULL, stderr=subprocess.STDOUT) if quiet else {}
+    subprocess.run(["make", "-s", "-C", HERE], check=True, **kw)
+
+
+_LIBS: dict = {}
+
+
+def have_reference() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _lib(kind: str):
+    if kind in _LIBS:
+        return _LIBS[kind]
+    path = PORT_LIB if kind == "port" else REF_LIB
+    if not os.path.exists(path):
+        if kind == "port":
+            build()
+        else:
+            raise FileNotFoundError(f"reference library not built: {path}")
+    lib = ctypes.CDLL(path)
+    i64, u64p, i64p = ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int64)
+    if kind == "port":
+        lib.oracle_connected_components.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, i64, i64, i64, i64, ctypes.c_int, ctypes.c_int,
+            ctypes.c_int, ctypes.c_void_p, ctypes.c_int, u64p]
+        lib.oracle_connected_components.restype = ctypes.c_int
+        lib.oracle_epl.argtypes = [ctypes.c_void_p, ctypes.c_int, i64, i64, i64p, i64p]
+        lib.oracle_epl.restype = ctypes.c_uint64
+    else:
+        lib.ref_connected_components.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, i64, i64, i64, i64, i64, ctypes.c_void_p,
+            ctypes.c_int, u64p, ctypes.c_int, ctypes.c_int]
+        lib.ref_connected_components.restype = ctypes.c_int
+        lib.ref_epl.argtypes = [ctypes.c_void_p, ctypes.c_int, i64, i64, i64p, i64p]
+        lib.ref_epl.restype = ctypes.c_uint64
+    _LIBS[kind] = lib
+    return lib
+
+
+def _core_dtype(dtype: np.dtype) -> np.dtype:
+    """The unsigned/float view the reference dispatches on (fastcc3d.pyx:494-608)."""
+    dtype = np.dtype(dtype)
+    if dtype == bool or dtype in (np.int8, np.uint8):
+        return np.dtype(np.uint8)
+    if dtype in (np.int16, np.uint16):
+        return np.dtype(np.uint16)
+    if dtype in (np.int32, np.uint32):
+        return np.dtype(np.uint32)
+    if dtype in (np.int64, np.uint64):
+        return np.dtype(np.uint64)
+    if dtype in (np.float32, np.float64):
+        return dtype
+    raise TypeError(
+        f"Type {dtype} is not currently supported. "
+        f"Supported: bool, int8, int16, int32, int64, uint8, uint16, uint32, uint64, float16, float32, float64"
+    )
+
+
+def _reshape_flat(arr: np.ndarray) -> np.ndarray:
+    """Memory-order flat view (fastcc3d.pyx:128-161 with shape=(size,))."""
+    if arr.flags.f_contiguous:
+        return arr.reshape(-1, order="F")
+    if arr.flags.c_contiguous:
+        return arr.reshape(-1, order="C")
+    return arr.reshape(-1)
+
+
+def estimate_provisional_labels(data: np.ndarray, backend: str = "port"):
+    """(epl, first_foreground_row, last_foreground_row); fastcc3d.pyx:168-242."""
+    sx = data.shape[0] if data.flags.f_contiguous else data.shape[-1]
+    linear = _reshape_flat(data)
+    cd = _core_dtype(data.dtype) if data.dtype != np.float16 else None
+    if cd is None:
+        raise TypeError(f"Type {data.dtype} is not currently supported.")
+    linear = np.ascontiguousarray(linear.view(cd))
+    first, last = ctypes.c_int64(0), ctypes.c_int64(0)
+    lib = _lib(backend)
+    fn = lib.oracle_epl if backend == "port" else lib.ref_epl
+    epl = fn(linear.ctypes.data, DT_CODES[cd], int(sx), int(linear.size),
+             ctypes.byref(first), ctypes.byref(last))
+    return (int(epl), int(first.value), int(last.value))
+
+
+def _even_ceil(n: int) -> int:
+    return n << 1 if n & 1 else n
+
+
+def _final_reshape(out, sx, sy, sz, dims, order):
+    """fastcc3d.pyx:628-642."""
+    if dims == 3:
+        return out.reshape((sz, sy, sx) if order == "C" else (sx, sy, sz), order=order)
+    if dims == 2:
+        return out.reshape((sy, sx) if order == "C" else (sx, sy), order=order)
+    return out.reshape((sx,), order=order)
+
+
+def _special_row(row_values: np.ndarray, out_row: np.ndarray) -> int:
+    """Run labelling of a single foreground row (fastcc3d.pyx:644-679).
+
+    The previous value is kept in a C int64: floats are truncated, and values
+    that do not fit raise like the reference does."""
+    N = 0
+    last = 0
+    for i, v in enumerate(row_values):
+        if v == 0:
+            last = 0
+            continue
+        if v == last:
+            out_row[i] = N
+            continue
+        N += 1
+        out_row[i] = N
+        if isinstance(v, (np.floating, float)):
+            fv = float(v)
+            if fv != fv:
+                raise ValueError("cannot convert float NaN to integer")
+            if fv in (float("inf"), float("-inf")) or not (-2**63 <= int(fv) < 2**63):
+                raise OverflowError("Python int too large to convert to C long")
+            last = int(fv)
+        else:
+            iv = int(v)
+            if not (-2**63 <= iv < 2**63):
+                raise OverflowError("Python int too large to convert to C long")
+            last = iv
+    return N
+
+
+def connected_components(data, max_labels=-1, connectivity=26, return_N=False,
+                         delta=0, out_dtype=None, out_file=None,
+                         periodic_boundary=False, binary_image=False,
+                         backend: str = "port"):
+    """Restatement of cc3d.connected_components (fastcc3d.pyx:244-626)."""
+    is_torch = hasattr(data, "cpu")
+    if is_torch:
+        data = data.cpu().numpy()
+    dims = len(data.shape)
+    if dims not in (1, 2, 3):
+        raise DimensionError("Only 1D, 2D, and 3D arrays supported. Got: " + str(dims))
+    if dims == 2 and connectivity not in (4, 8, 6, 18, 26):
+        raise ValueError("Only 4, 8, and 6, 18, 26 connectivities are supported for 2D images. Got: " + str(connectivity))
+    elif dims != 2 and connectivity not in (6, 18, 26):
+        raise ValueError("Only 6, 18, and 26 connectivities are supported for 3D images. Got: " + str(connectivity))
+    if periodic_boundary and connectivity not in (4, 8, 6):
+        raise ValueError(f"periodic_boundary is not yet implemented for {connectivity}-connectivity.")
+    if periodic_boundary and delta != 0:
+        raise ValueError("periodic_boundary is not yet implemented continuous data.")
+    if data.size == 0:
+        dtype = out_dtype if out_dtype is not None else data.dtype
+        out = np.zeros(shape=(0,), dtype=dtype)
+        return (out, 0) if return_N else out
+
+    order = "F" if data.flags.f_contiguous else "C"
+    while len(data.shape) < 3:
+        data = data[np.newaxis, ...] if order == "C" else data[..., np.newaxis]
+    if not data.flags.c_contiguous and not data.flags.f_contiguous:
+        data = np.copy(data, order=order)
+    if data.dtype == np.float16:
+        if delta == 0:
+            data = data.view(np.uint16)
+        else:
+            raise TypeError("float16 is not supported for continuous images (delta != 0).")
+    shape = list(data.shape)
+    if order == "C":
+        shape.reverse()
+    sx, sy, sz = shape
+    voxels = sx * sy * sz
+    dtype = data.dtype
+    binary_image = binary_image or (dtype == bool)
+    if binary_image:
+        epl, first_row, last_row = voxels, 0, sy
+    else:
+        epl, first_row, last_row = estimate_provisional_labels(data, backend=backend)
+    max_labels = min(epl, voxels)
+    if np.issubdtype(dtype, np.floating):
+        delta = float(delta)
+        binary_image = binary_image or (delta == np.finfo(dtype).max)
+    else:
+        delta = int(delta)
+        binary_image = binary_image or (delta == np.iinfo(dtype).max)
+    ufv = _even_ceil(data.shape[0]) * _even_ceil(data.shape[1]) * _even_ceil(data.shape[2])
+    if binary_image:
+        if connectivity in (4, 6):
+            max_labels = min(max_labels, (ufv // 2) + 1)
+        elif connectivity == (8, 18):  # never true: mirrors fastcc3d.pyx:412
+            max_labels = min(max_labels, (ufv // 4) + 1)
+        else:
+            max_labels = min(max_labels, (ufv // 8) + 1)
+    if out_dtype is not None:
+        out_dtype = np.dtype(out_dtype)
+        if out_dtype not in (np.uint16, np.uint32, np.uint64):
+            raise ValueError(
+                f"Explicitly defined out_dtype ({out_dtype}) must be one of: "
+                f"np.uint16, np.uint32, np.uint64")
+        if np.iinfo(out_dtype).max < max_labels:
+            raise ValueError(
+                f"Explicitly defined out_dtype ({out_dtype}) is too small "
+                f"to contain the estimated maximum number of labels ({max_labels}).")
+    elif max_labels < np.iinfo(np.uint16).max:
+        out_dtype = np.dtype(np.uint16)
+    elif max_labels < np.iinfo(np.uint32).max:
+        out_dtype = np.dtype(np.uint32)
+    else:
+        out_dtype = np.dtype(np.uint64)
+
+    if out_file is None:
+        out = np.zeros((voxels,), dtype=out_dtype, order="F")
+    else:
+        if isinstance(out_file, str):
+            with open(out_file, "wb") as f:
+                os.ftruncate(f.fileno(), voxels * np.dtype(out_dtype).itemsize)
+        out = np.memmap(out_file, order="F", dtype=out_dtype, shape=(voxels,))
+
+    if delta == 0 and first_row == last_row and first_row >= 0:
+        rz, ry = divmod(first_row, sy)
+        row = data[:, ry, rz] if data.flags.f_contiguous else data[rz, ry, :]
+        N = _special_row(row, out[first_row * sx:(first_row + 1) * sx])
+    else:
+        if delta != 0 and not binary_image:
+            raise NotImplementedError("continuous (delta != 0) labelling is not part of the oracle")
+        cd = _core_dtype(dtype)
+        flat = np.ascontiguousarray(_reshape_flat(data).view(cd))
+        n = ctypes.c_uint64(0)
+        odt = DT_CODES[out_dtype]
+        lib = _lib(backend)
+        if backend == "port":
+            rc = lib.oracle_connected_components(
+                flat.ctypes.data, DT_CODES[cd], sx, sy, sz, int(max_labels), int(connectivity),
+                int(bool(binary_image)), int(bool(periodic_boundary)),
+                out.ctypes.data, odt, ctypes.byref(n))
+        else:
+            rc = lib.ref_connected_components(
+                flat.ctypes.data, DT_CODES[cd], sx, sy, sz, int(max_labels),
+                int(connectivity), out.ctypes.data, odt, ctypes.byref(n),
+                int(bool(periodic_boundary)), int(bool(binary_image)))
+        if rc == -2 and backend == "port":
+            raise RuntimeError("sz must be 1 for 2D connectivities.")
+        if rc == -5 or (rc == -2 and backend == "reference"):
+            raise RuntimeError("maximum length exception")
+        if rc != 0:
+            raise RuntimeError(f"oracle failed with code {rc}")
+        N = int(n.value)
+
+    out = _final_reshape(out, sx, sy, sz, dims, order)
+    if is_torch:
+        import torch
+        out = torch.from_numpy(out)
+    return (out, N) if return_N else out
+
+
+def statistics(out_labels: np.ndarray, no_slice_conversion: bool = False) -> dict:
+    """numpy restatement of cc3d.statistics (fastcc3d.pyx:681-938)."""
+    while out_labels.ndim < 2:
+        out_labels = out_labels[..., np.newaxis]
+    if out_labels.dtype == bool:
+        out_labels = out_labels.view(np.uint8)
+    voxels = out_labels.size
+    if voxels == 0:
+        return {"voxel_counts": None, "bounding_boxes": None, "centroids": None}
+    if not (np.issubdtype(out_labels.dtype, np.integer)):
+        raise TypeError("Function call with ambiguous argument types")
+    N = int(np.max(out_labels))
+    if N > voxels:
+        raise ValueError(
+            f"Statistics can only be computed on volumes containing labels with values lower than the number of voxels. Max: {N}")
+    if np.issubdtype(out_labels.dtype, np.signedinteger):
+        mn = int(np.min(out_labels))
+        if mn < 0:
+            raise ValueError(
+                f"Statistics can only be computed on volumes containing labels with values >= 0. Min: {mn}")
+        out_labels = out_labels.view(f"u{out_labels.dtype.itemsize}")
+    ndim = out_labels.ndim
+    shape = out_labels.shape
+    bdt = np.uint32 if any(s > np.iinfo(np.uint16).max for s in (list(shape) + [1])[:3]) else np.uint16
+    idx = np.indices(shape, dtype=np.int64)
+    # labels and coordinates raveled in the same (C) order; integer sums are
+    # exact, so the accumulation order of the reference does not matter.
+    lab = out_labels.astype(np.int64).reshape(-1)
+    coords = [c.reshape(-1) for c in idx]
+    counts64 = np.bincount(lab, minlength=N + 1)
+    counts = counts64.astype(np.uint32)
+    bmax = np.iinfo(bdt).max
+    bb = np.zeros((N + 1, 2 * ndim), dtype=bdt)
+    cent = np.zeros((N + 1, ndim), dtype=np.float64)
+    for a in range(ndim):
+        mins = np.full(N + 1, bmax, dtype=np.int64)
+        maxs = np.zeros(N + 1, dtype=np.int64)
+        np.minimum.at(mins, lab, coords[a])
+        np.maximum.at(maxs, lab, coords[a])
+        bb[:, 2 * a] = mins.astype(bdt)
+        bb[:, 2 * a + 1] = maxs.astype(bdt)
+        s = np.zeros(N + 1, dtype=np.int64)
+        np.add.at(s, lab, coords[a])
+        cent[:, a] = s.astype(np.float64)
+    cnt_d = counts.astype(np.float64)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        cent = np.where(cnt_d[:, None] == 0, np.nan, cent / np.where(cnt_d == 0, 1, cnt_d)[:, None])
+    output = {"voxel_counts": counts, "bounding_boxes": bb, "centroids": cent}
+    if no_slice_conversion:
+        return output
+    slices = []
+    for row in bb:
+        starts = row[0::2]
+        ends = row[1::2]
+        if all(int(s) < voxels for s in starts):
+            slices.append(tuple(slice(int(s), int(e) + 1) for s, e in zip(starts, ends)))
+        else:
+            slices.append(None)
+    output["bounding_boxes"] = slices
+    return output

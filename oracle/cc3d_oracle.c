@@ -1,0 +1,380 @@
+/*
+ * cc3d_oracle.c -- CPU restatement of cc3d's labelling semantics.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU path: it is
+ * loaded by tests/, by __graft_entry__.smoke() and by the CPU-baseline leg of
+ * bench.py, and by nothing in the product.  It is pinned against the reference
+ * itself (oracle/_ref, the reference's own headers compiled by oracle/Makefile)
+ * and against the golden vectors in tests/golden/.
+ *
+ * What it restates (paths relative to the cc3d source tree):
+ *   - estimate_provisional_label_count   cc3d/cc3d.hpp:287-315
+ *   - the labelling contract of connected_components3d
+ *       dispatch                         cc3d/cc3d_continuous.hpp:394-455,
+ *                                        cc3d/cc3d.hpp:1423-1471,
+ *                                        cc3d/cc3d_binary.hpp:1266-1314
+ *       neighbourhoods                   26: cc3d/cc3d.hpp:372-399 (13-voxel backward mask)
+ *                                        18: cc3d/cc3d.hpp:597-755, 6: cc3d/cc3d.hpp:757-1076,
+ *                                        8: cc3d/cc3d.hpp:1287-1421, 4: cc3d/cc3d.hpp:1096-1280
+ *       periodic wrap pairs              6: cc3d/cc3d.hpp:1048-1073, 4: cc3d/cc3d.hpp:1265-1277,
+ *                                        8: cc3d/cc3d.hpp:1377-1418,
+ *                                        binary: cc3d/cc3d_binary.hpp:733-758, 938-950,
+ *                                        cc3d/cc3d_binary.hpp:1170-1210
+ *       numbering                        cc3d/cc3d.hpp:244-285 (relabel): components are
+ *                                        numbered 1..N in raster order of their first voxel;
+ *                                        binary 8-connected images use the 2x2-block
+ *                                        labeller (cc3d/cc3d_binary.hpp:955-1263), which
+ *                                        numbers components in block-raster order of their
+ *                                        first 2x2 block.
+ *
+ * The algorithm here is deliberately plain: one raster pass that unites every
+ * voxel with its equal-valued backward neighbours in a union-find whose root is
+ * always the minimum raster index, the periodic wrap pairs, then one raster pass
+ * that numbers roots.  Background voxels are written as 0.
+ *
+ * Known, documented difference: for binary 8-connected images whose memory
+ * dimensions are not both even, the reference's in-place relabel
+ * (cc3d/cc3d_binary.hpp:1237-1260) leaves provisional block labels in some
+ * background pixels outside each row's foreground span.  This oracle writes 0
+ * there, as the GPU path does; foreground pixels match exactly.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define DT_U8 1
+#define DT_U16 2
+#define DT_U32 3
+#define DT_U64 4
+#define DT_F32 5
+#define DT_F64 6
+
+static inline uint32_t uf_find(uint32_t *p, uint32_t i) {
+  while (p[i] != i) {
+    p[i] = p[p[i]];
+    i = p[i];
+  }
+  return i;
+}
+
+static inline uint32_t uf_unite(uint32_t *p, uint32_t a, uint32_t b) {
+  a = uf_find(p, a);
+  b = uf_find(p, b);
+  if (a == b) return a;
+  if (a < b) { p[b] = a; return a; }
+  p[a] = b;
+  return b;
+}
+
+/* backward offsets (dx, dy, dz) per connectivity */
+static const int OFF26[13][3] = {
+  {-1,-1,-1},{0,-1,-1},{1,-1,-1},{-1,0,-1},{0,0,-1},{1,0,-1},{-1,1,-1},{0,1,-1},{1,1,-1},
+  {-1,-1,0},{0,-1,0},{1,-1,0},{-1,0,0}};
+static const int OFF18[9][3] = {
+  {0,-1,-1},{-1,0,-1},{0,0,-1},{1,0,-1},{0,1,-1},{-1,-1,0},{0,-1,0},{1,-1,0},{-1,0,0}};
+static const int OFF6[3][3] = {{0,0,-1},{0,-1,0},{-1,0,0}};
+static const int OFF8[4][3] = {{-1,-1,0},{0,-1,0},{1,-1,0},{-1,0,0}};
+static const int OFF4[2][3] = {{0,-1,0},{-1,0,0}};
+
+static int offsets_for(int conn, const int (**off)[3]) {
+  switch (conn) {
+    case 26: *off = OFF26; return 13;
+    case 18: *off = OFF18; return 9;
+    case 6: *off = OFF6; return 3;
+    case 8: *off = OFF8; return 4;
+    case 4: *off = OFF4; return 2;
+  }
+  return -1;
+}
+
+/* ---- per-type kernels, generated by macro ---------------------------- */
+
+#define FG(v) ((v) != 0)
+#define EQV(a, b) (binary ? (FG(a) && FG(b)) : (FG(a) && (a) == (b)))
+
+#define DEFINE_TYPE(SUF, T)                                                     \
+static uint64_t epl_##SUF(const T *in, int64_t sx, int64_t voxels,              \
+                          int64_t *first, int64_t *last) {                      \
+  uint64_t count = 0;                                                           \
+  *first = -1; *last = -1;                                                      \
+  int64_t row = 0;                                                              \
+  for (int64_t loc = 0; loc < voxels; loc += sx, row++) {                       \
+    uint64_t rc = (in[loc] != 0);                                               \
+    for (int64_t x = 1; x < sx; x++)                                            \
+      rc += (in[loc + x] != in[loc + x - 1] && in[loc + x] != 0);               \
+    count += rc;                                                                \
+    if (rc) { if (*first == -1) *first = row; *last = row; }                    \
+  }                                                                             \
+  return count;                                                                 \
+}                                                                               \
+static void unite_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz,        \
+                        int conn, int binary, int periodic, uint32_t *par) {    \
+  const int (*off)[3];                                                          \
+  int noff = offsets_for(conn, &off);                                           \
+  const int64_t sxy = sx * sy;                                                  \
+  int64_t doff[13];                                                             \
+  /* binary 4-connected (cc3d/cc3d_binary.hpp:776-953): the first row links    \
+     horizontal neighbours only when their values are equal (:833), and later   \
+     rows skip the horizontal link when both pixels have foreground above      \
+     (the SIMPLE state, :903-918), relying on the row above being linked.      \
+     Together these define the reference's effective neighbour relation.     */ \
+  const int row0_eq = binary && conn == 4;                                      \
+  for (int k = 0; k < noff; k++)                                                \
+    doff[k] = off[k][0] + sx * off[k][1] + sxy * off[k][2];                     \
+  for (int64_t z = 0; z < sz; z++)                                              \
+    for (int64_t y = 0; y < sy; y++) {                                          \
+      int64_t row = sx * (y + sy * z);                                          \
+      int yz_in = (y >= 1) && (y + 1 < sy) && (z >= 1);                         \
+      for (int64_t x = 0; x < sx; x++) {                                        \
+        int64_t i = row + x;                                                    \
+        par[i] = (uint32_t)i;                                                   \
+        T v = in[i];                                                            \
+        if (!FG(v)) continue;                                                   \
+        int interior = yz_in && x >= 1 && x + 1 < sx;                           \
+        for (int k = 0; k < noff; k++) {                                        \
+          if (!interior) {                                                      \
+            int64_t nx = x + off[k][0], ny = y + off[k][1], nz = z + off[k][2]; \
+            if (nx < 0 || nx >= sx || ny < 0 || ny >= sy || nz < 0 || nz >= sz) \
+              continue;                                                         \
+          }                                                                     \
+          int64_t j = i + doff[k];                                              \
+          T w = in[j];                                                          \
+          if (row0_eq && off[k][1] == 0) {                                      \
+            if (y == 0) { if (v != w) continue; }                               \
+            else if (FG(in[i - sx]) && FG(in[j - sx])) continue;                \
+          }                                                                     \
+          if (EQV(v, w)) uf_unite(par, (uint32_t)i, (uint32_t)j);               \
+        }                                                                       \
+      }                                                                         \
+    }                                                                           \
+  if (!periodic) return;                                                        \
+  /* wrap pairs: x faces, y faces (with diagonals for 8), z faces, corners */   \
+  if (conn == 6 || conn == 4) {                                                 \
+    for (int64_t z = 0; z < sz; z++)                                            \
+      for (int64_t y = 0; y < sy; y++) {                                        \
+        int64_t a = sx * (y + sy * z), b = a + sx - 1;                          \
+        if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);         \
+      }                                                                         \
+    for (int64_t z = 0; z < sz; z++)                                            \
+      for (int64_t x = 0; x < sx; x++) {                                        \
+        int64_t a = x + sxy * z, b = a + sx * (sy - 1);                         \
+        if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);         \
+      }                                                                         \
+    if (conn == 6)                                                              \
+      for (int64_t y = 0; y < sy; y++)                                          \
+        for (int64_t x = 0; x < sx; x++) {                                      \
+          int64_t a = x + sx * y, b = a + sxy * (sz - 1);                       \
+          if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);       \
+        }                                                                       \
+  } else if (conn == 8) {                                                       \
+    const int64_t voxels = sx * sy;                                             \
+    const int64_t bot = sx * (sy - 1);                                          \
+    for (int64_t x = 0; x < sx; x++) {                                          \
+      if (!FG(in[x])) continue;                                                 \
+      if (x > 0 && EQV(in[x], in[x - 1 + bot]))                                 \
+        uf_unite(par, (uint32_t)x, (uint32_t)(x - 1 + bot));                    \
+      if (EQV(in[x], in[x + bot])) uf_unite(par, (uint32_t)x, (uint32_t)(x + bot)); \
+      if (x < sx - 1 && EQV(in[x], in[x + 1 + bot]))                            \
+        uf_unite(par, (uint32_t)x, (uint32_t)(x + 1 + bot));                    \
+    }                                                                           \
+    if (EQV(in[0], in[voxels - 1])) uf_unite(par, 0, (uint32_t)(voxels - 1));   \
+    if (EQV(in[sx - 1], in[bot])) uf_unite(par, (uint32_t)(sx - 1), (uint32_t)bot); \
+    for (int64_t y = 0; y < sy; y++) {                                          \
+      int64_t a = sx * y;                                                       \
+      if (!FG(in[a])) continue;                                                 \
+      if (EQV(in[a], in[a + sx - 1])) uf_unite(par, (uint32_t)a, (uint32_t)(a + sx - 1)); \
+      if (y > 0 && EQV(in[a], in[a - 1]))                                       \
+        uf_unite(par, (uint32_t)a, (uint32_t)(a - 1));                          \
+      if (y < sy - 1 && EQV(in[a], in[a + 2 * sx - 1]))                         \
+        uf_unite(par, (uint32_t)a, (uint32_t)(a + 2 * sx - 1));                 \
+    }                                                                           \
+  }                                                                             \
+}                                                                               \
+static int fg_##SUF(const void *in, int64_t i) { return FG(((const T *)in)[i]); } \
+/* Provisional labels the reference's binary labeller would create: a voxel  \
+   (or, for 8-connected, a 2x2 block) opens a new label iff none of its       \
+   backward-mask neighbours is foreground.                                   */ \
+static uint64_t prov_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz,     \
+                           int conn) {                                          \
+  uint64_t P = 0;                                                               \
+  if (conn == 8) {                                                              \
+    for (int64_t y = 0; y < sy; y += 2)                                         \
+      for (int64_t x = 0; x < sx; x += 2) {                                     \
+        int Y = FG(in[x + sx * y]);                                             \
+        int Z = x + 1 < sx && FG(in[x + 1 + sx * y]);                           \
+        int X = y + 1 < sy && FG(in[x + sx * (y + 1)]);                         \
+        int W = x + 1 < sx && y + 1 < sy && FG(in[x + 1 + sx * (y + 1)]);       \
+        if (!(Y || Z || X || W)) continue;                                      \
+        int up = y > 0;                                                         \
+        int C = up && x > 0 && FG(in[x - 1 + sx * (y - 1)]);                    \
+        int D = up && FG(in[x + sx * (y - 1)]);                                 \
+        int E = up && x + 1 < sx && FG(in[x + 1 + sx * (y - 1)]);               \
+        int F = up && x + 2 < sx && FG(in[x + 2 + sx * (y - 1)]);               \
+        int B = x > 0 && FG(in[x - 1 + sx * y]);                                \
+        int A = x > 0 && y + 1 < sy && FG(in[x - 1 + sx * (y + 1)]);            \
+        int linked = (Y && (C || D || E || B || A)) || (Z && (D || E || F)) ||  \
+                     (X && (B || A));                                           \
+        if (!linked) P++;                                                       \
+      }                                                                         \
+    return P;                                                                   \
+  }                                                                             \
+  const int (*off)[3];                                                          \
+  int noff = offsets_for(conn, &off);                                           \
+  for (int64_t z = 0; z < sz; z++)                                              \
+    for (int64_t y = 0; y < sy; y++)                                            \
+      for (int64_t x = 0; x < sx; x++) {                                        \
+        int64_t i = x + sx * (y + sy * z);                                      \
+        if (!FG(in[i])) continue;                                               \
+        int linked = 0;                                                         \
+        for (int k = 0; k < noff && !linked; k++) {                             \
+          int64_t nx = x + off[k][0], ny = y + off[k][1], nz = z + off[k][2];   \
+          if (nx < 0 || nx >= sx || ny < 0 || ny >= sy || nz < 0 || nz >= sz)   \
+            continue;                                                           \
+          T w = in[nx + sx * (ny + sy * nz)];                                   \
+          if (conn == 4 && y == 0 && off[k][1] == 0) linked = (w == in[i]);     \
+          else linked = FG(w);                                                  \
+        }                                                                       \
+        if (!linked) P++;                                                       \
+      }                                                                         \
+  return P;                                                                     \
+}
+
+DEFINE_TYPE(u8, uint8_t)
+DEFINE_TYPE(u16, uint16_t)
+DEFINE_TYPE(u32, uint32_t)
+DEFINE_TYPE(u64, uint64_t)
+DEFINE_TYPE(f32, float)
+DEFINE_TYPE(f64, double)
+
+static void store_label(void *out, int out_dtype, int64_t i, uint64_t lab) {
+  switch (out_dtype) {
+    case DT_U16: ((uint16_t *)out)[i] = (uint16_t)lab; break;
+    case DT_U32: ((uint32_t *)out)[i] = (uint32_t)lab; break;
+    default: ((uint64_t *)out)[i] = lab; break;
+  }
+}
+
+static uint64_t load_label(const void *out, int out_dtype, int64_t i) {
+  switch (out_dtype) {
+    case DT_U16: return ((const uint16_t *)out)[i];
+    case DT_U32: return ((const uint32_t *)out)[i];
+    default: return ((const uint64_t *)out)[i];
+  }
+}
+
+/* Estimated provisional label count and first/last foreground row
+ * (cc3d/cc3d.hpp:287-315).  Returns (uint64_t)-1 on an unknown dtype. */
+uint64_t oracle_epl(const void *in, int dtype, int64_t sx, int64_t voxels,
+                    int64_t *first, int64_t *last) {
+  switch (dtype) {
+    case DT_U8: return epl_u8((const uint8_t *)in, sx, voxels, first, last);
+    case DT_U16: return epl_u16((const uint16_t *)in, sx, voxels, first, last);
+    case DT_U32: return epl_u32((const uint32_t *)in, sx, voxels, first, last);
+    case DT_U64: return epl_u64((const uint64_t *)in, sx, voxels, first, last);
+    case DT_F32: return epl_f32((const float *)in, sx, voxels, first, last);
+    case DT_F64: return epl_f64((const double *)in, sx, voxels, first, last);
+  }
+  return (uint64_t)-1;
+}
+
+/* Label `in` (x fastest, sx*sy*sz voxels) into `out` (uint16/32/64 by
+ * out_dtype).  connectivity in {26,18,6} or {8,4} (sz must be 1).  Returns 0,
+ * -1 on bad arguments, -2 when sz != 1 for a 2D connectivity, -3 when the
+ * volume has 2^32 voxels or more, -4 on allocation failure, and -5 where the
+ * reference's binary labeller would overflow its union-find and throw
+ * "maximum length exception" (its table is sized from max_labels with
+ * per-labeller caps: cc3d/cc3d_binary.hpp:49-54, 350-354, 532-537, 795-800,
+ * 966-971; DisjointSet::add, cc3d/cc3d.hpp:106-115). */
+int oracle_connected_components(const void *in, int dtype, int64_t sx,
+                                int64_t sy, int64_t sz, int64_t max_labels,
+                                int connectivity, int binary, int periodic,
+                                void *out, int out_dtype, uint64_t *N) {
+  const int (*off)[3];
+  if (offsets_for(connectivity, &off) < 0) return -1;
+  if ((connectivity == 8 || connectivity == 4) && sz != 1) return -2;
+  const int64_t voxels = sx * sy * sz;
+  *N = 0;
+  if (voxels == 0) return 0;
+  if (voxels >= (int64_t)0xFFFFFFFFLL) return -3;
+  if (max_labels == 0) {
+    for (int64_t i = 0; i < voxels; i++) store_label(out, out_dtype, i, 0);
+    return 0;
+  }
+  if (binary) {
+    uint64_t P = 0;
+    switch (dtype) {
+      case DT_U8: P = prov_u8((const uint8_t *)in, sx, sy, sz, connectivity); break;
+      case DT_U16: P = prov_u16((const uint16_t *)in, sx, sy, sz, connectivity); break;
+      case DT_U32: P = prov_u32((const uint32_t *)in, sx, sy, sz, connectivity); break;
+      case DT_U64: P = prov_u64((const uint64_t *)in, sx, sy, sz, connectivity); break;
+      case DT_F32: P = prov_f32((const float *)in, sx, sy, sz, connectivity); break;
+      case DT_F64: P = prov_f64((const double *)in, sx, sy, sz, connectivity); break;
+    }
+    uint64_t L = (uint64_t)max_labels + 1, V = (uint64_t)voxels;
+    uint64_t outmax = out_dtype == DT_U16 ? 0xFFFFull : out_dtype == DT_U32 ? 0xFFFFFFFFull : ~0ull;
+    switch (connectivity) {
+      case 26: L = (L < (V >> 2) + 1 ? L : (V >> 2) + 1) + 1; break;
+      case 18: L = (L < V + 1 ? L : V + 1); break;
+      case 8: L = (L < (V >> 1) + 1 ? L : (V >> 1) + 1); if (L < 1) L = 1; L += 1; break;
+      default: L = (L < (V >> 1) + 1 ? L : (V >> 1) + 1) + 1; break;
+    }
+    if (L > outmax) L = outmax;
+    if (P >= L) return -5;
+  }
+  uint32_t *par = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+  if (!par) return -4;
+  int (*fg)(const void *, int64_t) = NULL;
+  switch (dtype) {
+#define CASE(D, SUF, T)                                                     \
+    case D:                                                                 \
+      unite_##SUF((const T *)in, sx, sy, sz, connectivity, binary,          \
+                  periodic, par);                                           \
+      fg = fg_##SUF;                                                        \
+      break;
+    CASE(DT_U8, u8, uint8_t)
+    CASE(DT_U16, u16, uint16_t)
+    CASE(DT_U32, u32, uint32_t)
+    CASE(DT_U64, u64, uint64_t)
+    CASE(DT_F32, f32, float)
+    CASE(DT_F64, f64, double)
+#undef CASE
+    default: free(par); return -1;
+  }
+  /* The parent of every non-root is smaller than the node itself (roots are
+     only ever linked under smaller roots), so one forward pass flattens every
+     tree: par[par[i]] is already the root when i is reached. */
+  for (int64_t i = 0; i < voxels; i++)
+    if (fg(in, i)) par[i] = par[par[i]];
+  uint64_t n = 0;
+  if (binary && connectivity == 8) {
+    /* block-raster numbering: visit 2x2 blocks in raster order; a component
+       takes its number at the first block that holds one of its pixels.  The
+       number is parked at the root's own slot of `out`. */
+    for (int64_t i = 0; i < voxels; i++) store_label(out, out_dtype, i, 0);
+    for (int64_t by = 0; by < sy; by += 2)
+      for (int64_t bx = 0; bx < sx; bx += 2)
+        for (int dy = 0; dy < 2; dy++)
+          for (int dx = 0; dx < 2; dx++) {
+            int64_t x = bx + dx, y = by + dy;
+            if (x >= sx || y >= sy) continue;
+            int64_t i = x + sx * y;
+            if (!fg(in, i)) continue;
+            uint32_t r = par[i];
+            if (load_label(out, out_dtype, r) == 0) store_label(out, out_dtype, r, ++n);
+          }
+    for (int64_t i = 0; i < voxels; i++)
+      if (fg(in, i)) store_label(out, out_dtype, i, load_label(out, out_dtype, par[i]));
+  } else {
+    /* raster numbering: the root of every tree is its minimum raster index,
+       i.e. the component's first voxel, so one forward pass numbers them. */
+    for (int64_t i = 0; i < voxels; i++) {
+      if (!fg(in, i)) { store_label(out, out_dtype, i, 0); continue; }
+      uint32_t r = par[i];
+      store_label(out, out_dtype, i,
+                  r == (uint32_t)i ? ++n : load_label(out, out_dtype, r));
+    }
+  }
+  free(par);
+  *N = n;
+  return 0;
+}

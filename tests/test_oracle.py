@@ -1,0 +1,63 @@
+"""The CPU oracle against the reference's golden vectors (and the compiled
+reference itself where it is available).  No GPU needed."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+import oracle
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    oracle.build()
+
+
+def test_golden_connected_components():
+    tally = {"ok": 0, "bg-defect": 0}
+    for i, m in G.cases("cc"):
+        tally[G.check_cc(i, m, oracle.connected_components)] += 1
+    assert tally["ok"] > 1000
+    # the documented binary-8 background difference stays rare
+    assert tally["bg-defect"] <= 0.05 * (tally["ok"] + tally["bg-defect"])
+
+
+def test_golden_epl():
+    for i, m in G.cases("epl"):
+        data = G.input_of(i, m)
+        if "exc" in m:
+            with pytest.raises(Exception) as ei:
+                oracle.estimate_provisional_labels(data)
+            assert type(ei.value).__name__ == m["exc"]
+        else:
+            assert list(oracle.estimate_provisional_labels(data)) == m["epl"], m["name"]
+
+
+def test_golden_statistics():
+    for i, m in G.cases("stats"):
+        G.check_stats(i, m, oracle.statistics)
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not compiled here")
+@pytest.mark.parametrize("seed", range(4))
+def test_port_matches_reference_random(seed):
+    rng = np.random.default_rng(seed)
+    for _ in range(60):
+        dims = int(rng.integers(2, 4))
+        shape = tuple(int(s) for s in rng.integers(1, 30 if dims == 2 else 12, dims))
+        a = (rng.integers(1, 4, shape) * (rng.random(shape) < rng.uniform(0.2, 0.8))).astype(np.uint16)
+        conn = int(rng.choice((4, 8, 6, 18, 26) if dims == 2 else (6, 18, 26)))
+        kw = dict(connectivity=conn, binary_image=bool(rng.random() < 0.3),
+                  periodic_boundary=bool(conn in (4, 8, 6) and rng.random() < 0.3))
+        try:
+            r = oracle.connected_components(a, return_N=True, backend="reference", **kw)
+        except RuntimeError:
+            with pytest.raises(RuntimeError):
+                oracle.connected_components(a, return_N=True, **kw)
+            continue
+        o = oracle.connected_components(a, return_N=True, **kw)
+        assert o[1] == r[1]
+        if kw["binary_image"] and conn == 8:
+            fg = a != 0
+            assert np.array_equal(o[0][fg], r[0][fg])
+        else:
+            assert np.array_equal(o[0], r[0])
