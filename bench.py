@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark of the labelling hot path (one JSON line on rank 0).
+
+Workload (one step): cc3d-style connected components of a 512^3 uint32
+Voronoi volume (4096 seeds, labels in [1, 2^20], one-voxel membrane, 2 % salt),
+26-connectivity: provisional-label estimate, labelling, numbering and the
+write of the uint32 output.  Inputs are synthetic and seeded.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl gb300 (default)
+    value  GVoxels/s with the input resident in HBM (CUDA tensor through the
+           public API, output allocated on the device).  The 512 MiB input is
+           larger than L2 (129 MB), so no flush is needed between steps.
+    e2e    the same metric through the C ABI with pinned host buffers: the
+           host->device copy of the input and the device->host copy of the
+           labels are inside the timed region.
+--impl reference
+    The reference's CPU implementation of the path on this machine's host
+    cores: the compiled reference where it was built here (oracle/_ref), else
+    the oracle's C restatement.  It is single-threaded.
+
+Multi-GPU (torchrun): every rank labels its own volume (replicas; the
+path has no data exchange), value = all voxels / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics as pystats
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "connected-components-3d_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "GVoxels/s 512^3 uint32 26-conn labelling (bit-exact)"
+SHAPE = (512, 512, 512)
+N_SEEDS = 4096
+LABEL_MAX = 1 << 20
+CONN = 26
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    self.samples.append(parts)
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for name, v in zip(names, s[5:9]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": pystats.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("CC3D_BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_volume(rank: int) -> np.ndarray:
+    from cc3d_gb300 import synth
+    return synth.voronoi_volume(SHAPE, N_SEEDS, LABEL_MAX, seed=1 + rank, dtype=np.uint32)
+
+
+def cpu_reference(vol: np.ndarray, budget_s: float = 20.0):
+    """Time the reference's CPU path (compiled reference if present, else the
+    oracle's C port) on the full workload volume, best of up to 3 runs."""
+    import oracle
+    oracle.build()
+    kind = "reference" if oracle.have_reference() else "port"
+    times = []
+    t_start = time.perf_counter()
+    N = None
+    while len(times) < 3 and (time.perf_counter() - t_start) < budget_s:
+        t0 = time.perf_counter()
+        _, N = oracle.connected_components(vol, connectivity=CONN, return_N=True, backend=kind)
+        times.append(time.perf_counter() - t0)
+    best = min(times)
+    return {"value": vol.size / best / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": kind,
+            "sample": f"full 512^3 uint32 volume, 26-conn, best of {len(times)} runs "
+                      f"({best:.3f} s per volume, N={N})"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    vol = make_volume(0)
+    times = []
+    import oracle
+    oracle.build()
+    kind = "reference" if oracle.have_reference() else "port"
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, N = oracle.connected_components(vol, connectivity=CONN, return_N=True, backend=kind)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    ms = 1000.0 * sum(times) / len(times)
+    value = vol.size / (ms / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded Voronoi)",
+        "config": {"workload": "512^3 uint32 Voronoi(4096 seeds)+membrane+2% salt, connectivity 26",
+                   "volumes_per_step": 1, "l2": "input larger than L2"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "GVoxels/s", "cores": 1, "kind": kind,
+                         "sample": "the full 512^3 volume per step (single-threaded CPU code)"},
+        "e2e": {"value": value, "unit": "GVoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import cc3d_gb300 as cc3d
+    cc3d.build()
+    nat = cc3d._native
+    lib = nat.load()
+
+    vol = make_volume(rank)
+    voxels = vol.size
+    dev = torch.from_numpy(vol).cuda()
+    # the expected N for this volume, from one labelled warm-up
+    out, N = cc3d.connected_components(dev, connectivity=CONN, return_N=True)
+    torch.cuda.synchronize()
+    out_dtype = out.dtype
+
+    # ---------------- device-resident value
+    for _ in range(args.warmup):
+        cc3d.connected_components(dev, connectivity=CONN, return_N=True)
+    torch.cuda.synchronize()
+    nat.profile_enable(True)
+    nat.profile_read()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_host0 = time.perf_counter()
+    ev0.record()
+    for _ in range(args.steps):
+        _, n = cc3d.connected_components(dev, connectivity=CONN, return_N=True)
+        assert n == N
+    ev1.record()
+    torch.cuda.synchronize()
+    t_host = time.perf_counter() - t_host0
+    barrier(world)
+    clocks = sampler.stop()
+    stage = nat.profile_read()
+    nat.profile_enable(False)
+    ms_total = ev0.elapsed_time(ev1)
+    ms_total = max_over_ranks(world, ms_total)
+    ms_per_step = ms_total / args.steps
+    value = world * voxels * args.steps / (ms_total / 1000.0) / 1e9
+
+    # ---------------- end to end through the C ABI with pinned host buffers
+    pin_in = torch.from_numpy(vol).pin_memory()
+    host_in = pin_in.numpy()
+    osz = {torch.uint16: 2, torch.uint32: 4, torch.uint64: 8}[out_dtype]
+    ocode = {2: nat.U16, 4: nat.U32, 8: nat.U64}[osz]
+    pin_out = torch.empty(voxels * osz, dtype=torch.uint8).pin_memory()
+    sx, sy, sz = SHAPE[2], SHAPE[1], SHAPE[0]
+
+    def e2e_step():
+        epl, first, last = ctypes.c_uint64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        nat.check(lib.cc3d_gpu_estimate_provisional_label_count(
+            host_in.ctypes.data, nat.U32, sx, voxels, ctypes.byref(epl), ctypes.byref(first),
+            ctypes.byref(last), 0, None))
+        n = ctypes.c_uint64(0)
+        nat.check(lib.cc3d_gpu_connected_components3d(
+            host_in.ctypes.data, nat.U32, sx, sy, sz, int(min(epl.value, voxels)), CONN, 0.0,
+            pin_out.data_ptr(), ocode, ctypes.byref(n), 0, 0, 0, None))
+        return n.value
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert e2e_step() == N
+    t_e2e = max_over_ranks(world, time.perf_counter() - t0)
+    e2e_value = world * voxels * args.steps / t_e2e / 1e9
+    expect = out.cpu().numpy().reshape(-1).view(np.uint8)
+    assert np.array_equal(pin_out.numpy(), expect), "e2e labels differ from the device path"
+
+    # ---------------- roofline of the dominant kernel
+    peak, peak_kind = load_peaks()
+    isz, osz_b = vol.itemsize, osz
+    kern_bytes = {
+        # algorithmic bytes per launch: the share of the job's (input + output)
+        # traffic the kernel is responsible for
+        "tile_local": voxels * isz,
+        "write": voxels * osz_b,
+        "epl": voxels * isz,
+    }
+    per_launch = {k: (stage[k][0] / stage[k][1] if stage[k][1] else 0.0) for k in stage}
+    dom = max(("tile_local", "write", "epl"), key=lambda k: per_launch[k])
+    dom_ms = per_launch[dom]
+    achieved = kern_bytes[dom] / (dom_ms / 1000.0) / 1e9 if dom_ms else 0.0
+    job_bytes = voxels * (isz + osz_b)
+    pipeline_gbs = job_bytes / (ms_per_step / 1000.0) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get(dom)
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = cpu_reference(vol)
+
+    launches_per_step = 7  # epl, tile_local, merge_edges, 3 scan kernels, write
+    line = {
+        "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded Voronoi; the reference publishes no number for this config)",
+        "config": {"workload": "512^3 uint32 Voronoi(4096 seeds, labels in [1,2^20])+membrane+2% salt, "
+                               "connectivity 26, output uint32",
+                   "volumes_per_step_per_gpu": 1, "N": N,
+                   "l2": "input (512 MiB) larger than L2, no flush"},
+        "e2e": {"value": e2e_value, "unit": "GVoxels/s",
+                "h2d_bytes_per_step": 2 * voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
+                "path": "C ABI, pinned host buffers, epl call + label call (input staged by each)"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kern_bytes[dom], "avg_launch_ms": dom_ms},
+        "pipeline_roofline": {"algorithmic_bytes_per_step": job_bytes, "achieved_gbs": pipeline_gbs,
+                              "frac": pipeline_gbs / peak,
+                              "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items() if v[1]}},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches_per_step * args.steps,
+        "host_wall_s": t_host,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

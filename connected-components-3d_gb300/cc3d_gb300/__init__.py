@@ -1,0 +1,22 @@
+"""cc3d_gb300 -- GB300 (sm_103a) implementation of cc3d's labelling path.
+
+Drop-in for ``cc3d.connected_components``, ``cc3d.statistics`` and
+``cc3d.estimate_provisional_labels``; the work runs in hand-written CUDA
+kernels behind the C ABI of include/cc3d_gpu.h (libcc3d_gpu.so).
+"""
+from ._build import build  # noqa: F401
+from .api import (  # noqa: F401
+    DimensionError,
+    connected_components,
+    estimate_provisional_labels,
+    statistics,
+)
+from . import _native  # noqa: F401
+
+__all__ = [
+    "build",
+    "connected_components",
+    "estimate_provisional_labels",
+    "statistics",
+    "DimensionError",
+]

@@ -1,0 +1,111 @@
+"""ctypes binding of libcc3d_gpu.so (the C ABI declared in include/cc3d_gpu.h).
+
+There is no CPU fallback: when the library is missing or no CUDA device is
+usable, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import _build
+
+U8, U16, U32, U64, F32, F64 = 1, 2, 3, 4, 5, 6
+IN_DEVICE, OUT_DEVICE = 1, 2
+
+OK = 0
+ERR_INVALID = -1
+ERR_UNSUPPORTED = -2
+ERR_CUDA = -3
+ERR_NOMEM = -4
+ERR_RUNTIME = -5
+ERR_DEVICE = -6
+ERR_OVERFLOW = -7
+ERR_NAN = -8
+
+EXPORTED = (
+    "cc3d_gpu_last_error",
+    "cc3d_gpu_version",
+    "cc3d_gpu_estimate_provisional_label_count",
+    "cc3d_gpu_connected_components3d",
+    "cc3d_gpu_special_row",
+    "cc3d_gpu_label_minmax",
+    "cc3d_gpu_statistics",
+    "cc3d_gpu_profile_enable",
+    "cc3d_gpu_profile_read",
+    "cc3d_gpu_release_workspace",
+)
+PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load() -> ctypes.CDLL:
+    """Load the native library (it must have been built: cc3d_gb300.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise ImportError(
+                f"the CUDA extension is not built ({path} is missing); "
+                "run cc3d_gb300.build() or __graft_entry__.build()")
+        lib = ctypes.CDLL(path)
+        vp, i64, u64p, i64p = ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int64)
+        ci = ctypes.c_int
+        lib.cc3d_gpu_last_error.restype = ctypes.c_char_p
+        lib.cc3d_gpu_version.restype = ctypes.c_char_p
+        lib.cc3d_gpu_estimate_provisional_label_count.argtypes = [vp, ci, i64, i64, u64p, i64p, i64p, ci, vp]
+        lib.cc3d_gpu_connected_components3d.argtypes = [
+            vp, ci, i64, i64, i64, i64, i64, ctypes.c_double, vp, ci, u64p, ci, ci, ci, vp]
+        lib.cc3d_gpu_special_row.argtypes = [vp, ci, ci, i64, i64, i64, i64, vp, ci, u64p, ci, vp]
+        lib.cc3d_gpu_label_minmax.argtypes = [vp, ci, ci, i64, u64p, i64p, ci, vp]
+        lib.cc3d_gpu_statistics.argtypes = [vp, ci, i64, i64, i64, ci, ci, ctypes.c_uint64, vp, vp, ci, vp, ci, vp]
+        lib.cc3d_gpu_release_workspace.restype = None
+        lib.cc3d_gpu_profile_enable.argtypes = [ci]
+        lib.cc3d_gpu_profile_enable.restype = None
+        lib.cc3d_gpu_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), u64p, ci]
+        for name in EXPORTED[2:7] + ("cc3d_gpu_profile_read",):
+            getattr(lib, name).restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def profile_enable(on: bool) -> None:
+    load().cc3d_gpu_profile_enable(int(bool(on)))
+
+
+def profile_read() -> dict:
+    """Per-stage (milliseconds, launches) accumulated since the last read."""
+    n = len(PROFILE_STAGES)
+    ms = (ctypes.c_double * n)()
+    cnt = (ctypes.c_uint64 * n)()
+    load().cc3d_gpu_profile_read(ms, cnt, n)
+    return {name: (ms[i], int(cnt[i])) for i, name in enumerate(PROFILE_STAGES)}
+
+
+def check(rc: int) -> None:
+    """Raise the Python exception the reference raises for this failure."""
+    if rc == OK:
+        return
+    msg = load().cc3d_gpu_last_error().decode(errors="replace")
+    if rc == ERR_INVALID:
+        raise ValueError(msg)
+    if rc == ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if rc == ERR_NOMEM:
+        raise MemoryError(msg)
+    if rc == ERR_OVERFLOW:
+        raise OverflowError(msg)
+    if rc == ERR_NAN:
+        raise ValueError(msg)
+    raise RuntimeError(msg)

@@ -1,0 +1,539 @@
+// cc3d_capi.cu -- host runtime behind include/cc3d_gpu.h.
+//
+// Owns the per-thread, per-device workspace (one grow-only device arena, a
+// pinned counter block and a private stream for host-buffer calls), validates
+// arguments like the reference's C++ entry points, stages host buffers, runs
+// the kernel pipeline on the caller's stream and maps device error words to
+// return codes.  No C++ exception crosses the ABI.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "cc3d_gpu.h"
+#include "cc3d_internal.h"
+
+using namespace cc3dgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) return fail(CC3D_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t dtype_size(int dt) {
+  switch (dt) {
+    case CC3D_U8: return 1;
+    case CC3D_U16: return 2;
+    case CC3D_U32: case CC3D_F32: return 4;
+    case CC3D_U64: case CC3D_F64: return 8;
+  }
+  return 0;
+}
+
+struct Profile {
+  bool on = false;
+  double ms[CC3D_PROFILE_STAGES] = {0};
+  uint64_t launches[CC3D_PROFILE_STAGES] = {0};
+};
+thread_local Profile g_prof;
+
+struct Workspace {
+  cudaEvent_t ev[CC3D_PROFILE_STAGES + 1] = {};
+  void* dev = nullptr;
+  size_t size = 0;
+  Counters* host_ctr = nullptr;
+  unsigned long long* host_small = nullptr;
+  cudaStream_t own = nullptr;
+};
+
+// one workspace per (thread, device); released explicitly or at process exit
+thread_local std::map<int, Workspace> g_ws;
+
+int get_ws(Workspace*& out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  Workspace& w = g_ws[dev];
+  if (!w.host_ctr) {
+    CK(cudaMallocHost((void**)&w.host_ctr, sizeof(Counters)));
+    CK(cudaMallocHost((void**)&w.host_small, 64));
+    CK(cudaStreamCreateWithFlags(&w.own, cudaStreamNonBlocking));
+    for (auto& e : w.ev) CK(cudaEventCreate(&e));
+  }
+  out = &w;
+  return CC3D_OK;
+}
+
+int reserve(Workspace& w, size_t bytes) {
+  if (bytes <= w.size) return CC3D_OK;
+  if (w.dev) {
+    cudaFree(w.dev);
+    w.dev = nullptr;
+    w.size = 0;
+  }
+  size_t want = bytes + bytes / 8 + (64u << 20);
+  cudaError_t e = cudaMalloc(&w.dev, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&w.dev, bytes);
+    want = bytes;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    w.dev = nullptr;
+    return fail(CC3D_ERR_NOMEM, "cannot allocate %zu bytes of device workspace", bytes);
+  }
+  w.size = want;
+  return CC3D_OK;
+}
+
+// carves aligned sub-buffers out of the arena
+struct Carver {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    const size_t at = off;
+    off += (bytes + 255) & ~size_t(255);
+    return at;
+  }
+};
+
+cudaStream_t pick_stream(Workspace& w, void* stream, int mem_flags) {
+  if (stream) return (cudaStream_t)stream;
+  return mem_flags ? (cudaStream_t)0 : w.own;
+}
+
+int check_device_errors(unsigned err) {
+  if (!err) return CC3D_OK;
+  return fail(CC3D_ERR_DEVICE,
+              "device kernel gave up (error bits 0x%x: %s%s%s%s)", err,
+              (err & ERR_UNITE_BUDGET) ? "union budget " : "",
+              (err & ERR_FIND_BUDGET) ? "find budget " : "",
+              (err & ERR_EDGE_OVERFLOW) ? "edge buffer overflow " : "",
+              (err & ERR_LOCAL_BUDGET) ? "tile union budget" : "");
+}
+
+Counters fresh_counters() {
+  Counters c;
+  memset(&c, 0, sizeof(c));
+  c.first_row = 0x7FFFFFFFFFFFFFFFLL;
+  c.last_row = -1;
+  return c;
+}
+
+#define DISPATCH_DTYPE(dt, FN, ...)                  \
+  ([&]() -> cudaError_t {                            \
+    switch (dt) {                                    \
+      case CC3D_U8: return FN##_u8(__VA_ARGS__);     \
+      case CC3D_U16: return FN##_u16(__VA_ARGS__);   \
+      case CC3D_U32: return FN##_u32(__VA_ARGS__);   \
+      case CC3D_U64: return FN##_u64(__VA_ARGS__);   \
+      case CC3D_F32: return FN##_f32(__VA_ARGS__);   \
+      case CC3D_F64: return FN##_f64(__VA_ARGS__);   \
+    }                                                \
+    return cudaErrorInvalidValue;                    \
+  }())
+
+// Stage timer: mark(k) records the end of stage k (the start is the previous
+// mark); finish() adds the elapsed times of the marked stages after the
+// stream has been synchronised.
+struct StageTimer {
+  Workspace& w;
+  cudaStream_t s;
+  int last = -1;
+  int order[CC3D_PROFILE_STAGES + 1];
+  int n = 0;
+  StageTimer(Workspace& w_, cudaStream_t s_) : w(w_), s(s_) {
+    if (g_prof.on) { cudaEventRecord(w.ev[0], s); order[n++] = -1; }
+  }
+  void mark(int stage) {
+    if (!g_prof.on || n > CC3D_PROFILE_STAGES) return;
+    cudaEventRecord(w.ev[n], s);
+    order[n++] = stage;
+  }
+  void finish() {
+    if (!g_prof.on) return;
+    for (int i = 1; i < n; ++i) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, w.ev[i - 1], w.ev[i]) == cudaSuccess) {
+        g_prof.ms[order[i]] += ms;
+        g_prof.launches[order[i]] += 1;
+      }
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+void cc3d_gpu_profile_enable(int enable) { g_prof.on = enable != 0; }
+
+int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n) {
+  if (n > CC3D_PROFILE_STAGES) n = CC3D_PROFILE_STAGES;
+  for (int i = 0; i < n; ++i) {
+    if (ms) ms[i] = g_prof.ms[i];
+    if (launches) launches[i] = g_prof.launches[i];
+    g_prof.ms[i] = 0;
+    g_prof.launches[i] = 0;
+  }
+  return n;
+}
+
+const char* cc3d_gpu_last_error(void) { return g_err.c_str(); }
+
+const char* cc3d_gpu_version(void) { return "cc3d-gb300 0.1 (sm_103a)"; }
+
+void cc3d_gpu_release_workspace(void) {
+  for (auto& kv : g_ws) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(kv.first);
+    if (kv.second.dev) cudaFree(kv.second.dev);
+    if (kv.second.host_ctr) cudaFreeHost(kv.second.host_ctr);
+    if (kv.second.host_small) cudaFreeHost(kv.second.host_small);
+    if (kv.second.own) cudaStreamDestroy(kv.second.own);
+    cudaSetDevice(prev);
+  }
+  g_ws.clear();
+}
+
+int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t sx, int64_t voxels,
+                                              uint64_t* epl, int64_t* first_row,
+                                              int64_t* last_row, int mem_flags, void* stream) {
+  const size_t isz = dtype_size(dtype);
+  if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
+  if (sx < 0 || voxels < 0 || !epl || !first_row || !last_row)
+    return fail(CC3D_ERR_INVALID, "invalid arguments");
+  if (voxels == 0 || sx == 0) {
+    *epl = 0;
+    *first_row = -1;
+    *last_row = -1;
+    return CC3D_OK;
+  }
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+  Carver cv;
+  const size_t o_ctr = cv.take(sizeof(Counters));
+  const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);
+  const size_t o_in = stage_in ? cv.take(voxels * isz) : 0;
+  if (int rc = reserve(*w, cv.off)) return rc;
+  char* base = (char*)w->dev;
+  Counters* ctr = (Counters*)(base + o_ctr);
+  *w->host_ctr = fresh_counters();
+  CK(cudaMemcpyAsync(ctr, w->host_ctr, sizeof(Counters), cudaMemcpyHostToDevice, s));
+  StageTimer tm(*w, s);
+  const void* din = in;
+  if (stage_in) {
+    CK(cudaMemcpyAsync(base + o_in, in, voxels * isz, cudaMemcpyHostToDevice, s));
+    din = base + o_in;
+    tm.mark(0);
+  }
+  CK(DISPATCH_DTYPE(dtype, launch_epl, din, sx, voxels, ctr, s));
+  tm.mark(1);
+  CK(cudaMemcpyAsync(w->host_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  tm.finish();
+  *epl = w->host_ctr->epl;
+  *first_row = w->host_ctr->epl ? w->host_ctr->first_row : -1;
+  *last_row = w->host_ctr->epl ? w->host_ctr->last_row : -1;
+  return CC3D_OK;
+}
+
+int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                                    int64_t max_labels, int64_t connectivity, double delta,
+                                    void* out, int out_dtype, uint64_t* N, int periodic_boundary,
+                                    int binary_image, int mem_flags, void* stream) {
+  const size_t isz = dtype_size(dtype);
+  if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
+  if (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64)
+    return fail(CC3D_ERR_INVALID, "out_dtype must be uint16, uint32 or uint64 (code %d)", out_dtype);
+  const size_t osz = dtype_size(out_dtype);
+  if (sx < 0 || sy < 0 || sz < 0 || !N) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  const int conn = (int)connectivity;
+  if (conn != 26 && conn != 18 && conn != 6 && conn != 8 && conn != 4)
+    return fail(CC3D_ERR_RUNTIME, "Only 4 and 8 2D and 6, 18, and 26 3D connectivities are supported.");
+  if ((conn == 8 || conn == 4) && sz != 1)
+    return fail(CC3D_ERR_RUNTIME, "sz must be 1 for 2D connectivities.");
+  if (delta != 0.0 && !binary_image)
+    return fail(CC3D_ERR_UNSUPPORTED, "continuous-value labelling (delta != 0) is not implemented");
+  if (periodic_boundary && conn != 4 && conn != 8 && conn != 6)
+    return fail(CC3D_ERR_INVALID, "periodic_boundary is only implemented for 4, 8 and 6 connectivity");
+  *N = 0;
+  const int64_t voxels = sx * sy * sz;
+  if (voxels == 0) return CC3D_OK;
+
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+
+  if (max_labels == 0) {  // the reference returns before labelling
+    if (mem_flags & CC3D_OUT_DEVICE) {
+      CK(cudaMemsetAsync(out, 0, voxels * osz, s));
+      CK(cudaStreamSynchronize(s));
+    } else {
+      memset(out, 0, voxels * osz);
+    }
+    return CC3D_OK;
+  }
+
+  // effective neighbourhood: a single z plane makes 26/18 equal to 8 and 6 to 4
+  int eff = conn;
+  if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
+  if (sz == 1 && conn == 6) eff = 4;
+  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
+  const bool block8 = binary_image && conn == 8;
+  const bool d3 = (eff == 26 || eff == 18 || eff == 6);
+  const int TY = d3 ? 8 : 64, TZ = d3 ? 8 : 1, HZ = d3 ? 1 : 0;
+
+  LabelArgs a;
+  memset(&a, 0, sizeof(a));
+  a.sx = sx; a.sy = sy; a.sz = sz;
+  a.ntx = (int)((sx + kTX - 1) / kTX);
+  a.nty = (int)((sy + TY - 1) / TY);
+  a.ntz = (int)((sz + TZ - 1) / TZ);
+  a.ty = TY; a.tz = TZ;
+  const int64_t ntiles = (int64_t)a.ntx * a.nty * a.ntz;
+  if (ntiles * kTV >= 0xFFFFFFFFLL)
+    return fail(CC3D_ERR_UNSUPPORTED, "volume too large: %lld tiles of 2048 voxels exceed 32-bit node ids",
+                (long long)ntiles);
+  int64_t nwords;
+  if (block8) {
+    const int64_t osx = (sx + 1) >> 1, osy = (sy + 1) >> 1;
+    a.wpr = (osx + 31) / 32;
+    a.key_row = a.wpr * 32;
+    nwords = osy * a.wpr;
+  } else {
+    a.wpr = a.ntx;
+    a.key_row = a.wpr * 32;
+    nwords = sy * sz * a.wpr;
+  }
+  if (nwords * 32 >= 0xFFFFFFFFLL)
+    return fail(CC3D_ERR_UNSUPPORTED, "volume too large for 32-bit component keys");
+  const int64_t halo = (int64_t)(kTX + 2) * (TY + 2) * (TZ + HZ) - kTV;
+  const int64_t edge_cap64 = ntiles * halo;
+  a.edge_cap = (unsigned)(edge_cap64 > 0xFFFFFFF0LL ? 0xFFFFFFF0LL : edge_cap64);
+  a.want_epl = 0;
+  a.want_prov = binary_image ? 1 : 0;
+
+  const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);
+  const bool stage_out = !(mem_flags & CC3D_OUT_DEVICE);
+  const int64_t nblocks = scan_blocks_needed(nwords);
+  Carver cv;
+  const size_t o_ctr = cv.take(sizeof(Counters));
+  const size_t o_in = stage_in ? cv.take(voxels * isz) : 0;
+  const size_t o_out = stage_out ? cv.take(voxels * osz) : 0;
+  const size_t o_rec = cv.take(ntiles * kTV * sizeof(uint16_t));
+  const size_t o_E = cv.take(ntiles * kTV * sizeof(unsigned long long));
+  const size_t o_cc = cv.take(ntiles * sizeof(uint32_t));
+  const size_t o_bm = cv.take(nwords * sizeof(uint32_t));
+  const size_t o_pf = cv.take(nwords * sizeof(uint32_t));
+  const size_t o_bs = cv.take((nblocks + 1) * sizeof(uint32_t));
+  const size_t o_ed = cv.take((size_t)a.edge_cap * sizeof(uint2));
+  if (int rc = reserve(*w, cv.off)) return rc;
+  char* base = (char*)w->dev;
+  Counters* ctr = (Counters*)(base + o_ctr);
+  a.ctr = ctr;
+  a.rec = (uint16_t*)(base + o_rec);
+  a.E = (unsigned long long*)(base + o_E);
+  a.ccount = (uint32_t*)(base + o_cc);
+  a.bitmap = (uint32_t*)(base + o_bm);
+  a.prefix = (uint32_t*)(base + o_pf);
+  a.edges = (uint2*)(base + o_ed);
+  uint32_t* bsum = (uint32_t*)(base + o_bs);
+
+  *w->host_ctr = fresh_counters();
+  CK(cudaMemcpyAsync(ctr, w->host_ctr, sizeof(Counters), cudaMemcpyHostToDevice, s));
+  if (block8) CK(cudaMemsetAsync(a.bitmap, 0, nwords * sizeof(uint32_t), s));
+  StageTimer tm(*w, s);
+  a.in = in;
+  if (stage_in) {
+    CK(cudaMemcpyAsync(base + o_in, in, voxels * isz, cudaMemcpyHostToDevice, s));
+    a.in = base + o_in;
+    tm.mark(0);
+  }
+  void* dout = stage_out ? (void*)(base + o_out) : out;
+
+  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, ntiles, s));
+  tm.mark(2);
+  CK(launch_merge_edges(a, s));
+  tm.mark(3);
+  if (periodic_boundary) {
+    CK(DISPATCH_DTYPE(dtype, launch_wrap, a, eff, mode, s));
+    tm.mark(4);
+  }
+  CK(launch_scan(a, nwords, bsum, nblocks, s));
+  tm.mark(5);
+  CK(launch_write(a, dout, out_dtype, ntiles, s));
+  tm.mark(6);
+  if (stage_out) {
+    CK(cudaMemcpyAsync(out, dout, voxels * osz, cudaMemcpyDeviceToHost, s));
+    tm.mark(7);
+  }
+  CK(cudaMemcpyAsync(w->host_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  tm.finish();
+  const Counters& h = *w->host_ctr;
+  if (int rc = check_device_errors(h.err)) return rc;
+  if (binary_image) {
+    // the reference's binary labellers size their union-find from max_labels
+    // with per-labeller caps and throw when a provisional label reaches it
+    const uint64_t V = (uint64_t)voxels;
+    uint64_t L = (uint64_t)max_labels + 1;
+    switch (conn) {
+      case 26: L = (L < (V >> 2) + 1 ? L : (V >> 2) + 1) + 1; break;
+      case 18: L = (L < V + 1 ? L : V + 1); break;
+      case 8: L = (L < (V >> 1) + 1 ? L : (V >> 1) + 1); if (L < 1) L = 1; L += 1; break;
+      default: L = (L < (V >> 1) + 1 ? L : (V >> 1) + 1) + 1; break;
+    }
+    const uint64_t outmax = out_dtype == CC3D_U16 ? 0xFFFFull : out_dtype == CC3D_U32 ? 0xFFFFFFFFull : ~0ull;
+    if (L > outmax) L = outmax;
+    if (h.prov >= L) return fail(CC3D_ERR_RUNTIME, "maximum length exception");
+  }
+  *N = h.N;
+  return CC3D_OK;
+}
+
+int cc3d_gpu_special_row(const void* in, int dtype, int is_uint64, int64_t sx, int64_t sy, int64_t sz,
+                         int64_t row, void* out, int out_dtype, uint64_t* N, int mem_flags,
+                         void* stream) {
+  const size_t isz = dtype_size(dtype), osz = dtype_size(out_dtype);
+  if (!isz || (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64) || !N)
+    return fail(CC3D_ERR_INVALID, "invalid arguments");
+  if (row < 0 || row >= sy * sz) return fail(CC3D_ERR_INVALID, "row %lld out of range", (long long)row);
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+  const bool stage_in = !(mem_flags & CC3D_IN_DEVICE), stage_out = !(mem_flags & CC3D_OUT_DEVICE);
+  Carver cv;
+  const size_t o_ctr = cv.take(sizeof(Counters));
+  const size_t o_in = stage_in ? cv.take(sx * isz) : 0;
+  const size_t o_out = stage_out ? cv.take(sx * osz) : 0;
+  if (int rc = reserve(*w, cv.off)) return rc;
+  char* base = (char*)w->dev;
+  Counters* ctr = (Counters*)(base + o_ctr);
+  *w->host_ctr = fresh_counters();
+  CK(cudaMemcpyAsync(ctr, w->host_ctr, sizeof(Counters), cudaMemcpyHostToDevice, s));
+  const char* rin = (const char*)in + row * sx * isz;
+  char* rout = (char*)out + row * sx * osz;
+  const void* din = rin;
+  void* dout = rout;
+  if (stage_in) {
+    CK(cudaMemcpyAsync(base + o_in, rin, sx * isz, cudaMemcpyHostToDevice, s));
+    din = base + o_in;
+  }
+  if (stage_out) {
+    CK(cudaMemcpyAsync(base + o_out, rout, sx * osz, cudaMemcpyHostToDevice, s));
+    dout = base + o_out;
+  }
+  CK(DISPATCH_DTYPE(dtype, launch_special_row, din, sx, 0, is_uint64, dout, out_dtype, ctr, s));
+  if (stage_out) CK(cudaMemcpyAsync(rout, dout, sx * osz, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(w->host_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const unsigned err = w->host_ctr->err;
+  if (err & 16u) return fail(CC3D_ERR_NAN, "cannot convert float NaN to integer");
+  if (err & 32u) return fail(CC3D_ERR_OVERFLOW, "Python int too large to convert to C long");
+  *N = w->host_ctr->N;
+  return CC3D_OK;
+}
+
+int cc3d_gpu_label_minmax(const void* labels, int dtype, int is_signed, int64_t voxels, uint64_t* vmax,
+                          int64_t* vmin, int mem_flags, void* stream) {
+  const size_t isz = dtype_size(dtype);
+  if (!isz || dtype == CC3D_F32 || dtype == CC3D_F64 || !vmax || !vmin || voxels <= 0)
+    return fail(CC3D_ERR_INVALID, "invalid arguments");
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+  const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);
+  Carver cv;
+  const size_t o_res = cv.take(16);
+  const size_t o_in = stage_in ? cv.take(voxels * isz) : 0;
+  if (int rc = reserve(*w, cv.off)) return rc;
+  char* base = (char*)w->dev;
+  unsigned long long* res = (unsigned long long*)(base + o_res);
+  const void* din = labels;
+  if (stage_in) {
+    CK(cudaMemcpyAsync(base + o_in, labels, voxels * isz, cudaMemcpyHostToDevice, s));
+    din = base + o_in;
+  }
+  CK(DISPATCH_DTYPE(dtype, launch_minmax, din, voxels, is_signed, res, s));
+  CK(cudaMemcpyAsync(w->host_small, res, 16, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *vmax = w->host_small[0];
+  *vmin = (int64_t)w->host_small[1];
+  return CC3D_OK;
+}
+
+int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, int64_t d2, int ndim,
+                        int c_order, uint64_t N, uint32_t* counts, void* bboxes, int bbox_dtype,
+                        double* centroids, int mem_flags, void* stream) {
+  const size_t isz = dtype_size(dtype);
+  if (!isz || dtype == CC3D_F32 || dtype == CC3D_F64)
+    return fail(CC3D_ERR_INVALID, "statistics needs unsigned integer labels");
+  if ((ndim != 2 && ndim != 3) || d0 <= 0 || d1 <= 0 || d2 <= 0 || (ndim == 2 && d2 != 1))
+    return fail(CC3D_ERR_INVALID, "invalid shape");
+  if (bbox_dtype != CC3D_U16 && bbox_dtype != CC3D_U32) return fail(CC3D_ERR_INVALID, "bbox dtype");
+  const int64_t voxels = d0 * d1 * d2;
+  if (N > (uint64_t)voxels) return fail(CC3D_ERR_INVALID, "N exceeds the voxel count");
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+  const int64_t n1 = (int64_t)N + 1;
+  const bool stage_in = !(mem_flags & CC3D_IN_DEVICE), stage_out = !(mem_flags & CC3D_OUT_DEVICE);
+  const size_t bsz = dtype_size(bbox_dtype);
+  Carver cv;
+  const size_t o_in = stage_in ? cv.take(voxels * isz) : 0;
+  const size_t o_cnt = cv.take(n1 * 4);
+  const size_t o_min = cv.take(n1 * 3 * 4);
+  const size_t o_max = cv.take(n1 * 3 * 4);
+  const size_t o_sum = cv.take(n1 * 3 * 8);
+  const size_t o_bb = stage_out ? cv.take(n1 * 2 * ndim * bsz) : 0;
+  const size_t o_ce = stage_out ? cv.take(n1 * ndim * 8) : 0;
+  if (int rc = reserve(*w, cv.off)) return rc;
+  char* base = (char*)w->dev;
+  StatsArgs a;
+  a.labels = labels;
+  if (stage_in) {
+    CK(cudaMemcpyAsync(base + o_in, labels, voxels * isz, cudaMemcpyHostToDevice, s));
+    a.labels = base + o_in;
+  }
+  a.dtype = dtype;
+  a.d0 = d0; a.d1 = d1; a.d2 = d2;
+  a.ndim = ndim;
+  a.c_order = c_order;
+  a.N = N;
+  a.counts = (stage_out ? (uint32_t*)(base + o_cnt) : counts);
+  a.bmin = (uint32_t*)(base + o_min);
+  a.bmax = (uint32_t*)(base + o_max);
+  a.sums = (unsigned long long*)(base + o_sum);
+  void* dbb = stage_out ? (void*)(base + o_bb) : bboxes;
+  double* dce = stage_out ? (double*)(base + o_ce) : centroids;
+  CK(launch_stats(a, s));
+  CK(launch_stats_finalize(a, dbb, bbox_dtype, dce, s));
+  if (stage_out) {
+    CK(cudaMemcpyAsync(counts, a.counts, n1 * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bboxes, dbb, n1 * 2 * ndim * bsz, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(centroids, dce, n1 * ndim * 8, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return CC3D_OK;
+}
+
+}  // extern "C"

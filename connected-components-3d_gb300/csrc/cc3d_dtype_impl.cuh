@@ -1,0 +1,269 @@
+// cc3d_dtype_impl.cuh -- element-type dependent kernels and their launchers.
+// Included once per element type by label_<type>.cu, which instantiates the
+// launchers declared in cc3d_internal.h through CC3D_DEFINE_DTYPE_LAUNCHERS.
+#pragma once
+
+#include "cc3d_internal.h"
+
+namespace cc3dgpu {
+
+constexpr unsigned ERR_NAN = 16u;
+constexpr unsigned ERR_OVERFLOW = 32u;
+
+// ------------------------------------------------------------------ epl
+// Provisional-label estimate: per row, [v[0] != 0] + #{x >= 1 : v[x] != v[x-1]
+// and v[x] != 0}, and the first/last row holding foreground
+// (cc3d/cc3d.hpp:287-315).  Work items are 1024-voxel segments of rows.
+template <typename T>
+__global__ void __launch_bounds__(256) k_epl(const T* in, int64_t sx, int64_t rows, Counters* ctr) {
+  constexpr int SEG = 1024;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t segs = (sx + SEG - 1) / SEG;
+  const int64_t items = rows * segs;
+  unsigned long long acc = 0;
+  long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+  for (int64_t it = (int64_t)blockIdx.x * 8 + warp; it < items; it += (int64_t)gridDim.x * 8) {
+    const int64_t row = it / segs, seg = it % segs;
+    const T* rp = in + row * sx;
+    const int64_t xs = seg * SEG, xe = (xs + SEG < sx) ? xs + SEG : sx;
+    T carry = (xs > 0) ? rp[xs - 1] : T(0);
+    unsigned cnt = 0;
+    for (int64_t xb = xs; xb < xe; xb += 32) {
+      const int64_t x = xb + lane;
+      const T v = (x < xe) ? rp[x] : T(0);
+      T prev = __shfl_up_sync(FULL, v, 1);
+      if (lane == 0) prev = carry;
+      cnt += __popc(__ballot_sync(FULL, (x < xe) && (v != prev) && (v != T(0))));
+      carry = __shfl_sync(FULL, v, 31);
+    }
+    if (cnt) {
+      acc += cnt;
+      f = row < f ? row : f;
+      l = row > l ? row : l;
+    }
+  }
+  __shared__ unsigned long long sa[8];
+  __shared__ long long sf[8], sl[8];
+  if (lane == 0) { sa[warp] = acc; sf[warp] = f; sl[warp] = l; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long a = 0;
+    for (int w = 0; w < 8; ++w) {
+      a += sa[w];
+      f = sf[w] < f ? sf[w] : f;
+      l = sl[w] > l ? sl[w] : l;
+    }
+    if (a) {
+      atomicAdd(&ctr->epl, a);
+      atomicMin(&ctr->first_row, f);
+      atomicMax(&ctr->last_row, l);
+    }
+  }
+}
+
+// ------------------------------------------------------------ special row
+// Single foreground row, labelled run by run with the previous run's value
+// held as a C int64, exactly like the reference's Python loop
+// (cc3d/fastcc3d.pyx:644-679).  Sequential by nature (a run continues while
+// values equal the truncated value that opened it), so one thread does it.
+template <typename T>
+__device__ __forceinline__ bool to_int64(T v, int is_uint64, long long& out, unsigned& err) {
+  if (sizeof(T) == 8 && (T)0.5 == T(0) && is_uint64) {  // unsigned 64-bit input
+    if ((unsigned long long)v >= 0x8000000000000000ull) { err |= ERR_OVERFLOW; return false; }
+    out = (long long)v;
+    return true;
+  }
+  if ((T)0.5 != T(0)) {  // floating point
+    const double d = (double)v;
+    if (d != d) { err |= ERR_NAN; return false; }
+    if (!(d > -9223372036854775809.0 && d < 9223372036854775808.0)) { err |= ERR_OVERFLOW; return false; }
+    out = (long long)d;  // truncation, like Python's int()
+    return true;
+  }
+  out = (long long)v;
+  return true;
+}
+
+template <typename T, typename OUT>
+__global__ void k_special_row(const T* in, int64_t sx, int64_t row, int is_uint64, OUT* out,
+                              Counters* ctr) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const T* rp = in + row * sx;
+  OUT* op = out + row * sx;
+  unsigned long long N = 0;
+  long long last = 0;
+  unsigned err = 0;
+  const bool is_float = (T)0.5 != T(0);
+  for (int64_t i = 0; i < sx; ++i) {
+    const T v = rp[i];
+    if (v == T(0)) { last = 0; continue; }
+    const bool same = is_float ? ((double)v == (double)last)
+                               : ((unsigned long long)v == (unsigned long long)last);
+    if (same) { op[i] = (OUT)N; continue; }
+    ++N;
+    op[i] = (OUT)N;
+    if (!to_int64<T>(v, is_uint64, last, err)) break;
+  }
+  ctr->N = N;
+  if (err) atomicOr(&ctr->err, err);
+}
+
+// ----------------------------------------------------------------- minmax
+template <typename T>
+__global__ void k_minmax_init(unsigned long long* res, int is_signed) {
+  if (is_signed) {
+    ((long long*)res)[0] = (long long)0x8000000000000000ull;
+    ((long long*)res)[1] = 0x7FFFFFFFFFFFFFFFLL;
+  } else {
+    res[0] = 0;
+    res[1] = ~0ull;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_minmax(const T* in, int64_t n, int is_signed,
+                                                unsigned long long* res) {
+  using ST = typename std::conditional<sizeof(T) == 1, int8_t,
+             typename std::conditional<sizeof(T) == 2, int16_t,
+             typename std::conditional<sizeof(T) == 4, int32_t, int64_t>::type>::type>::type;
+  long long smax = (long long)0x8000000000000000ull, smin = 0x7FFFFFFFFFFFFFFFLL;
+  unsigned long long umax = 0, umin = ~0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T v = in[i];
+    if (is_signed) {
+      ST s;
+      memcpy(&s, &v, sizeof(T));
+      const long long w = (long long)s;
+      smax = w > smax ? w : smax;
+      smin = w < smin ? w : smin;
+    } else {
+      const unsigned long long w = (unsigned long long)v;
+      umax = w > umax ? w : umax;
+      umin = w < umin ? w : umin;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    smax = max(smax, (long long)__shfl_down_sync(FULL, smax, o));
+    smin = min(smin, (long long)__shfl_down_sync(FULL, smin, o));
+    umax = max(umax, (unsigned long long)__shfl_down_sync(FULL, umax, o));
+    umin = min(umin, (unsigned long long)__shfl_down_sync(FULL, umin, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (is_signed) {
+      atomicMax((long long*)res, smax);
+      atomicMin((long long*)res + 1, smin);
+    } else {
+      atomicMax(res, umax);
+      atomicMin(res + 1, umin);
+    }
+  }
+}
+
+// ------------------------------------------------------------- launchers
+template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
+cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  k_tile_local<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool block8,
+                                int64_t ntiles, cudaStream_t s) {
+  switch (conn) {
+    case 26:
+      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
+      return mode == MODE_MULTI ? launch_k1<T, 26, 8, 8, MODE_MULTI, false>(a, ntiles, s)
+                                : launch_k1<T, 26, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+    case 18:
+      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
+      return mode == MODE_MULTI ? launch_k1<T, 18, 8, 8, MODE_MULTI, false>(a, ntiles, s)
+                                : launch_k1<T, 18, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+    case 6:
+      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
+      return mode == MODE_MULTI ? launch_k1<T, 6, 8, 8, MODE_MULTI, false>(a, ntiles, s)
+                                : launch_k1<T, 6, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+    case 8:
+      if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
+      if (mode == MODE_MULTI) return launch_k1<T, 8, 64, 1, MODE_MULTI, false>(a, ntiles, s);
+      if (block8) return launch_k1<T, 8, 64, 1, MODE_BINARY, true>(a, ntiles, s);
+      return launch_k1<T, 8, 64, 1, MODE_BINARY, false>(a, ntiles, s);
+    case 4:
+      if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
+      if (mode == MODE_MULTI) return launch_k1<T, 4, 64, 1, MODE_MULTI, false>(a, ntiles, s);
+      if (mode == MODE_BINARY4) return launch_k1<T, 4, 64, 1, MODE_BINARY4, false>(a, ntiles, s);
+      return launch_k1<T, 4, 64, 1, MODE_BINARY, false>(a, ntiles, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t launch_wrap_t(const LabelArgs& a, int conn, int mode, cudaStream_t s) {
+  const int64_t n = a.sy * a.sz + a.sx * a.sz + (conn == 6 ? a.sx * a.sy : 0) + 2;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (mode == MODE_MULTI) k_wrap_pairs<T, MODE_MULTI><<<(unsigned)blocks, 256, 0, s>>>(a, conn);
+  else k_wrap_pairs<T, MODE_BINARY><<<(unsigned)blocks, 256, 0, s>>>(a, conn);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_epl_t(const void* in, int64_t sx, int64_t voxels, Counters* ctr, cudaStream_t s) {
+  const int64_t rows = sx ? voxels / sx : 0;
+  const int64_t items = rows * ((sx + 1023) / 1024);
+  int64_t blocks = (items + 7) / 8;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  k_epl<T><<<(unsigned)blocks, 256, 0, s>>>(static_cast<const T*>(in), sx, rows, ctr);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_special_row_t(const void* in, int64_t sx, int64_t row, int is_uint64, void* out,
+                                 int out_dtype, Counters* ctr, cudaStream_t s) {
+  const T* tin = static_cast<const T*>(in);
+  switch (out_dtype) {
+    case 2: k_special_row<T, uint16_t><<<1, 1, 0, s>>>(tin, sx, row, is_uint64, (uint16_t*)out, ctr); break;
+    case 3: k_special_row<T, uint32_t><<<1, 1, 0, s>>>(tin, sx, row, is_uint64, (uint32_t*)out, ctr); break;
+    case 4: k_special_row<T, uint64_t><<<1, 1, 0, s>>>(tin, sx, row, is_uint64, (uint64_t*)out, ctr); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_minmax_t(const void* in, int64_t n, int is_signed, unsigned long long* res,
+                            cudaStream_t s) {
+  k_minmax_init<T><<<1, 1, 0, s>>>(res, is_signed);
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_minmax<T><<<(unsigned)blocks, 256, 0, s>>>(static_cast<const T*>(in), n, is_signed, res);
+  return cudaGetLastError();
+}
+
+}  // namespace cc3dgpu
+
+#define CC3D_DEFINE_DTYPE_LAUNCHERS(SUF, T)                                               \
+  namespace cc3dgpu {                                                                     \
+  cudaError_t launch_tile_local_##SUF(const LabelArgs& a, int conn, int mode, bool block8,  \
+                                      int64_t ntiles, cudaStream_t s) {                   \
+    return launch_tile_local_t<T>(a, conn, mode, block8, ntiles, s);                      \
+  }                                                                                       \
+  cudaError_t launch_wrap_##SUF(const LabelArgs& a, int conn, int mode, cudaStream_t s) { \
+    return launch_wrap_t<T>(a, conn, mode, s);                                            \
+  }                                                                                       \
+  cudaError_t launch_epl_##SUF(const void* in, int64_t sx, int64_t voxels, Counters* ctr, \
+                               cudaStream_t s) {                                          \
+    return launch_epl_t<T>(in, sx, voxels, ctr, s);                                       \
+  }                                                                                       \
+  cudaError_t launch_special_row_##SUF(const void* in, int64_t sx, int64_t row,          \
+                                       int is_uint64, void* out, int out_dtype,           \
+                                       Counters* ctr, cudaStream_t s) {                   \
+    return launch_special_row_t<T>(in, sx, row, is_uint64, out, out_dtype, ctr, s);       \
+  }                                                                                       \
+  cudaError_t launch_minmax_##SUF(const void* in, int64_t n, int is_signed,               \
+                                  unsigned long long* res, cudaStream_t s) {              \
+    return launch_minmax_t<T>(in, n, is_signed, res, s);                                  \
+  }                                                                                       \
+  }

@@ -1,0 +1,159 @@
+/*
+ * cc3d_gpu.h -- C ABI of the GB300 labelling core (libcc3d_gpu.so).
+ *
+ * Drop-in boundary for cc3d's labelling hot path.  Each entry point names the
+ * reference interface it replaces (paths relative to the cc3d source tree).
+ * Plain pointers and sizes only; no exceptions cross this boundary.
+ *
+ * Conventions
+ *   - Return CC3D_OK (0) or a negative CC3D_ERR_*; cc3d_gpu_last_error()
+ *     returns the message of the last failure on the calling thread.
+ *   - Volumes are raster ordered with x fastest: voxel (x, y, z) lives at
+ *     x + sx * (y + sy * z), as the reference's C++ core sees them after the
+ *     Cython layer has reversed C-order shapes (cc3d/fastcc3d.pyx:352-359).
+ *   - `mem_flags` says where each buffer lives: CC3D_IN_DEVICE and/or
+ *     CC3D_OUT_DEVICE.  Host buffers are staged through device memory owned by
+ *     the library; device buffers are used in place.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     ordered on that stream and return after the results they report (N,
+ *     counts, errors) are known, so host output buffers are filled on return.
+ *   - Calls may come from several host threads at once: every thread uses its
+ *     own device workspace.
+ *   - Volumes whose row-padded voxel count (ceil(sx/32)*32 * sy * sz) reaches
+ *     2^32 are rejected with CC3D_ERR_UNSUPPORTED.
+ */
+#ifndef CC3D_GPU_H
+#define CC3D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* element types (signed integers are passed as the unsigned type of the same
+   width, float16 as uint16, bool as uint8, exactly as the reference's Cython
+   layer views them: cc3d/fastcc3d.pyx:346-350, 494-608) */
+#define CC3D_U8 1
+#define CC3D_U16 2
+#define CC3D_U32 3
+#define CC3D_U64 4
+#define CC3D_F32 5
+#define CC3D_F64 6
+
+#define CC3D_IN_DEVICE 1
+#define CC3D_OUT_DEVICE 2
+
+#define CC3D_OK 0
+#define CC3D_ERR_INVALID -1      /* bad argument (ValueError in cc3d)              */
+#define CC3D_ERR_UNSUPPORTED -2  /* outside what this library implements            */
+#define CC3D_ERR_CUDA -3         /* a CUDA runtime call failed                       */
+#define CC3D_ERR_NOMEM -4        /* device allocation failed                         */
+#define CC3D_ERR_RUNTIME -5      /* the reference's std::runtime_error cases         */
+#define CC3D_ERR_DEVICE -6       /* a kernel gave up (iteration budget) and reported */
+#define CC3D_ERR_OVERFLOW -7     /* value does not fit a C int64 (OverflowError)     */
+#define CC3D_ERR_NAN -8          /* NaN where the reference converts to int64        */
+
+const char* cc3d_gpu_last_error(void);
+const char* cc3d_gpu_version(void);
+
+/*
+ * Estimated provisional label count and first/last foreground row.
+ * Replaces cc3d::estimate_provisional_label_count<T>
+ * (cc3d/cc3d.hpp:287-315; bound at cc3d/fastcc3d.pyx:60-65, called from
+ * estimate_provisional_labels, cc3d/fastcc3d.pyx:168-242).
+ * first_row / last_row are -1 when there is no foreground.
+ */
+int cc3d_gpu_estimate_provisional_label_count(
+    const void* in, int dtype, int64_t sx, int64_t voxels,
+    uint64_t* epl, int64_t* first_row, int64_t* last_row,
+    int mem_flags, void* stream);
+
+/*
+ * Connected components of `in` into `out` (uint16/32/64 by out_dtype).
+ * Replaces cc3d::connected_components3d<T,OUT>(in, sx, sy, sz, max_labels,
+ * connectivity, delta, out, N, periodic_boundary, binary_image)
+ * (cc3d/cc3d_continuous.hpp:394-455; bound at cc3d/fastcc3d.pyx:67-74).
+ *   connectivity: 26, 18, 6, or 8, 4 (the latter two need sz == 1, else
+ *                 CC3D_ERR_RUNTIME "sz must be 1 for 2D connectivities.").
+ *   max_labels:   the Cython layer's estimate; it only matters for binary
+ *                 images, where the reference's union-find is sized from it
+ *                 and throws "maximum length exception" when too small -- this
+ *                 library reports that case as CC3D_ERR_RUNTIME too.
+ *   delta:        must be 0 unless binary_image (continuous labelling,
+ *                 cc3d/cc3d_continuous.hpp:90-392, is not implemented).
+ * Labels are numbered 1..N in raster order of each component's first voxel;
+ * binary 8-connected images are numbered in raster order of each component's
+ * first 2x2 block, as the reference's block labeller does.  Background is 0.
+ */
+int cc3d_gpu_connected_components3d(
+    const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+    int64_t max_labels, int64_t connectivity, double delta,
+    void* out, int out_dtype, uint64_t* N,
+    int periodic_boundary, int binary_image,
+    int mem_flags, void* stream);
+
+/*
+ * The single-foreground-row case of the Cython layer: the foreground row
+ * `row` (0-based over sy*sz rows) is labelled run by run, keeping the previous
+ * run's value in a C int64 as the reference does.  Writes only that row of
+ * `out` (the caller zero-fills the rest, as np.zeros does in the reference).
+ * Replaces epl_special_row (cc3d/fastcc3d.pyx:644-679, called at :469-470).
+ * Returns CC3D_ERR_NAN / CC3D_ERR_OVERFLOW where the reference raises
+ * ValueError / OverflowError converting a run value to int64; `is_uint64`
+ * marks unsigned 64-bit input (values >= 2^63 overflow).
+ */
+int cc3d_gpu_special_row(
+    const void* in, int dtype, int is_uint64, int64_t sx, int64_t sy, int64_t sz,
+    int64_t row, void* out, int out_dtype, uint64_t* N, int mem_flags, void* stream);
+
+/*
+ * Largest and smallest label value (the N and sign checks of statistics,
+ * cc3d/fastcc3d.pyx:731-747).  `is_signed` interprets the element bits as
+ * two's complement; results are returned as int64 bit patterns in *vmax/*vmin
+ * (for unsigned 64-bit input *vmax is the raw uint64 value).
+ */
+int cc3d_gpu_label_minmax(
+    const void* labels, int dtype, int is_signed, int64_t voxels,
+    uint64_t* vmax, int64_t* vmin, int mem_flags, void* stream);
+
+/*
+ * Per-label voxel counts, bounding boxes and centroids.
+ * Replaces _statistics_helper2d/_statistics_helper3d
+ * (cc3d/fastcc3d.pyx:767-844, 846-938).
+ *   Dimensions d0, d1, d2 are the numpy axes (x = axis 0, y = axis 1,
+ *   z = axis 2; d2 = 1 and ndim = 2 for images); `c_order` says whether the
+ *   last axis (1) or the first axis (0) is fastest in memory.
+ *   counts:    uint32[N+1]
+ *   bboxes:    uint16 or uint32 (bbox_dtype CC3D_U16/CC3D_U32) [N+1][2*ndim],
+ *              (min, max) per axis; mins start at the type's maximum.
+ *   centroids: float64 [N+1][ndim]; NaN where the count is 0.
+ * Output buffers are host or device memory per CC3D_OUT_DEVICE.
+ */
+int cc3d_gpu_statistics(
+    const void* labels, int dtype, int64_t d0, int64_t d1, int64_t d2,
+    int ndim, int c_order, uint64_t N,
+    uint32_t* counts, void* bboxes, int bbox_dtype, double* centroids,
+    int mem_flags, void* stream);
+
+/*
+ * Per-stage timing of this thread's calls, measured with CUDA events on the
+ * call's own stream (no reference counterpart: the reference has no device
+ * stages).  While enabled, every call adds the milliseconds of each stage to
+ * the accumulators below; cc3d_gpu_profile_read copies them (and the number
+ * of launches of each stage) and resets them.
+ * Stage order: 0 h2d, 1 epl, 2 tile_local, 3 merge_edges, 4 wrap_pairs,
+ *              5 scan, 6 write, 7 d2h.
+ */
+#define CC3D_PROFILE_STAGES 8
+void cc3d_gpu_profile_enable(int enable);
+int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
+
+/* Release this thread's cached device workspace. */
+void cc3d_gpu_release_workspace(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CC3D_GPU_H */
