@@ -27,10 +27,12 @@
  *                                        numbers components in block-raster order of their
  *                                        first 2x2 block.
  *
- * The algorithm here is deliberately plain: one raster pass that unites every
- * voxel with its equal-valued backward neighbours in a union-find whose root is
- * always the minimum raster index, the periodic wrap pairs, then one raster pass
- * that numbers roots.  Background voxels are written as 0.
+ * The algorithm is the classic two-pass scheme the reference also uses: a
+ * raster pass assigns provisional labels (copying a matching backward
+ * neighbour's label, uniting differing ones in a union-find over labels whose
+ * root is the smallest label), the periodic wrap pairs are united, and a second
+ * pass writes each voxel's component number.  Background voxels are written as
+ * 0.  It is single-threaded, like the reference.
  *
  * Known, documented difference: for binary 8-connected images whose memory
  * dimensions are not both even, the reference's in-place relabel
@@ -57,12 +59,33 @@ static inline uint32_t uf_find(uint32_t *p, uint32_t i) {
   return i;
 }
 
-static inline uint32_t uf_unite(uint32_t *p, uint32_t a, uint32_t b) {
-  a = uf_find(p, a);
-  b = uf_find(p, b);
+/* union-find over provisional labels 1..n; the root of a set is its
+   smallest label, so a parent is always smaller than its child. */
+typedef struct {
+  uint32_t *par;
+  uint32_t n, cap;
+  int oom;
+} Labels;
+
+static uint32_t lab_new(Labels *L) {
+  if (L->n + 1 >= L->cap) {
+    uint32_t nc = L->cap ? L->cap * 2 : 1024;
+    uint32_t *np_ = (uint32_t *)realloc(L->par, sizeof(uint32_t) * nc);
+    if (!np_) { L->oom = 1; return L->n; }
+    L->par = np_;
+    L->cap = nc;
+  }
+  L->n++;
+  L->par[L->n] = L->n;
+  return L->n;
+}
+
+static uint32_t lab_unite(Labels *L, uint32_t a, uint32_t b) {
+  a = uf_find(L->par, a);
+  b = uf_find(L->par, b);
   if (a == b) return a;
-  if (a < b) { p[b] = a; return a; }
-  p[a] = b;
+  if (a < b) { L->par[b] = a; return a; }
+  L->par[a] = b;
   return b;
 }
 
@@ -107,30 +130,44 @@ static uint64_t epl_##SUF(const T *in, int64_t sx, int64_t voxels,              
   }                                                                             \
   return count;                                                                 \
 }                                                                               \
-static void unite_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz,        \
-                        int conn, int binary, int periodic, uint32_t *par) {    \
+/* Two-pass labelling with provisional labels, as the reference does: the   \
+   first raster pass copies a matching backward neighbour's label (or opens  \
+   a new one) and unites differing labels in a union-find over labels whose  \
+   root is always the smallest label; periodic wrap pairs are united next.   \
+   For 26-connectivity a voxel equal to the voxel below it (z-1) takes that  \
+   label and needs no other test: every other backward neighbour it relates  \
+   to is also a 26-neighbour of the voxel below, and that pair was already   \
+   united earlier in the scan.  Returns the number of provisional labels.   */ \
+static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz, \
+                                 int conn, int binary, int periodic,            \
+                                 uint32_t *lab, Labels *L) {                    \
   const int (*off)[3];                                                          \
   int noff = offsets_for(conn, &off);                                           \
   const int64_t sxy = sx * sy;                                                  \
   int64_t doff[13];                                                             \
+  for (int k = 0; k < noff; k++)                                                \
+    doff[k] = off[k][0] + sx * off[k][1] + sxy * off[k][2];                     \
   /* binary 4-connected (cc3d/cc3d_binary.hpp:776-953): the first row links    \
      horizontal neighbours only when their values are equal (:833), and later   \
      rows skip the horizontal link when both pixels have foreground above      \
      (the SIMPLE state, :903-918), relying on the row above being linked.      \
      Together these define the reference's effective neighbour relation.     */ \
   const int row0_eq = binary && conn == 4;                                      \
-  for (int k = 0; k < noff; k++)                                                \
-    doff[k] = off[k][0] + sx * off[k][1] + sxy * off[k][2];                     \
+  const int below_shortcut = (conn == 26);                                      \
   for (int64_t z = 0; z < sz; z++)                                              \
     for (int64_t y = 0; y < sy; y++) {                                          \
       int64_t row = sx * (y + sy * z);                                          \
       int yz_in = (y >= 1) && (y + 1 < sy) && (z >= 1);                         \
       for (int64_t x = 0; x < sx; x++) {                                        \
         int64_t i = row + x;                                                    \
-        par[i] = (uint32_t)i;                                                   \
         T v = in[i];                                                            \
-        if (!FG(v)) continue;                                                   \
+        if (!FG(v)) { lab[i] = 0; continue; }                                   \
+        if (below_shortcut && z > 0 && EQV(v, in[i - sxy])) {                   \
+          lab[i] = lab[i - sxy];                                                \
+          continue;                                                             \
+        }                                                                       \
         int interior = yz_in && x >= 1 && x + 1 < sx;                           \
+        uint32_t cur = 0;                                                       \
         for (int k = 0; k < noff; k++) {                                        \
           if (!interior) {                                                      \
             int64_t nx = x + off[k][0], ny = y + off[k][1], nz = z + off[k][2]; \
@@ -139,56 +176,61 @@ static void unite_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz,        
           }                                                                     \
           int64_t j = i + doff[k];                                              \
           T w = in[j];                                                          \
+          if (!EQV(v, w)) continue;                                             \
           if (row0_eq && off[k][1] == 0) {                                      \
             if (y == 0) { if (v != w) continue; }                               \
             else if (FG(in[i - sx]) && FG(in[j - sx])) continue;                \
           }                                                                     \
-          if (EQV(v, w)) uf_unite(par, (uint32_t)i, (uint32_t)j);               \
+          uint32_t l = lab[j];                                                  \
+          if (cur == 0) cur = l;                                                \
+          else if (l != cur) cur = lab_unite(L, cur, l);                        \
         }                                                                       \
+        if (cur == 0) cur = lab_new(L);                                         \
+        lab[i] = cur;                                                           \
       }                                                                         \
     }                                                                           \
-  if (!periodic) return;                                                        \
-  /* wrap pairs: x faces, y faces (with diagonals for 8), z faces, corners */   \
-  if (conn == 6 || conn == 4) {                                                 \
-    for (int64_t z = 0; z < sz; z++)                                            \
-      for (int64_t y = 0; y < sy; y++) {                                        \
-        int64_t a = sx * (y + sy * z), b = a + sx - 1;                          \
-        if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);         \
-      }                                                                         \
-    for (int64_t z = 0; z < sz; z++)                                            \
-      for (int64_t x = 0; x < sx; x++) {                                        \
-        int64_t a = x + sxy * z, b = a + sx * (sy - 1);                         \
-        if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);         \
-      }                                                                         \
-    if (conn == 6)                                                              \
-      for (int64_t y = 0; y < sy; y++)                                          \
+  if (periodic) {                                                               \
+    /* wrap pairs: x faces, y faces (with diagonals for 8), z faces, corners */ \
+    if (conn == 6 || conn == 4) {                                               \
+      for (int64_t z = 0; z < sz; z++)                                          \
+        for (int64_t y = 0; y < sy; y++) {                                      \
+          int64_t a = sx * (y + sy * z), b = a + sx - 1;                        \
+          if (EQV(in[a], in[b])) lab_unite(L, lab[a], lab[b]);                  \
+        }                                                                       \
+      for (int64_t z = 0; z < sz; z++)                                          \
         for (int64_t x = 0; x < sx; x++) {                                      \
-          int64_t a = x + sx * y, b = a + sxy * (sz - 1);                       \
-          if (EQV(in[a], in[b])) uf_unite(par, (uint32_t)a, (uint32_t)b);       \
+          int64_t a = x + sxy * z, b = a + sx * (sy - 1);                       \
+          if (EQV(in[a], in[b])) lab_unite(L, lab[a], lab[b]);                  \
         }                                                                       \
-  } else if (conn == 8) {                                                       \
-    const int64_t voxels = sx * sy;                                             \
-    const int64_t bot = sx * (sy - 1);                                          \
-    for (int64_t x = 0; x < sx; x++) {                                          \
-      if (!FG(in[x])) continue;                                                 \
-      if (x > 0 && EQV(in[x], in[x - 1 + bot]))                                 \
-        uf_unite(par, (uint32_t)x, (uint32_t)(x - 1 + bot));                    \
-      if (EQV(in[x], in[x + bot])) uf_unite(par, (uint32_t)x, (uint32_t)(x + bot)); \
-      if (x < sx - 1 && EQV(in[x], in[x + 1 + bot]))                            \
-        uf_unite(par, (uint32_t)x, (uint32_t)(x + 1 + bot));                    \
-    }                                                                           \
-    if (EQV(in[0], in[voxels - 1])) uf_unite(par, 0, (uint32_t)(voxels - 1));   \
-    if (EQV(in[sx - 1], in[bot])) uf_unite(par, (uint32_t)(sx - 1), (uint32_t)bot); \
-    for (int64_t y = 0; y < sy; y++) {                                          \
-      int64_t a = sx * y;                                                       \
-      if (!FG(in[a])) continue;                                                 \
-      if (EQV(in[a], in[a + sx - 1])) uf_unite(par, (uint32_t)a, (uint32_t)(a + sx - 1)); \
-      if (y > 0 && EQV(in[a], in[a - 1]))                                       \
-        uf_unite(par, (uint32_t)a, (uint32_t)(a - 1));                          \
-      if (y < sy - 1 && EQV(in[a], in[a + 2 * sx - 1]))                         \
-        uf_unite(par, (uint32_t)a, (uint32_t)(a + 2 * sx - 1));                 \
+      if (conn == 6)                                                            \
+        for (int64_t y = 0; y < sy; y++)                                        \
+          for (int64_t x = 0; x < sx; x++) {                                    \
+            int64_t a = x + sx * y, b = a + sxy * (sz - 1);                     \
+            if (EQV(in[a], in[b])) lab_unite(L, lab[a], lab[b]);                \
+          }                                                                     \
+    } else if (conn == 8) {                                                     \
+      const int64_t voxels = sx * sy;                                           \
+      const int64_t bot = sx * (sy - 1);                                        \
+      for (int64_t x = 0; x < sx; x++) {                                        \
+        if (!FG(in[x])) continue;                                               \
+        if (x > 0 && EQV(in[x], in[x - 1 + bot])) lab_unite(L, lab[x], lab[x - 1 + bot]); \
+        if (EQV(in[x], in[x + bot])) lab_unite(L, lab[x], lab[x + bot]);       \
+        if (x < sx - 1 && EQV(in[x], in[x + 1 + bot]))                          \
+          lab_unite(L, lab[x], lab[x + 1 + bot]);                               \
+      }                                                                         \
+      if (EQV(in[0], in[voxels - 1])) lab_unite(L, lab[0], lab[voxels - 1]);   \
+      if (EQV(in[sx - 1], in[bot])) lab_unite(L, lab[sx - 1], lab[bot]);       \
+      for (int64_t y = 0; y < sy; y++) {                                        \
+        int64_t a = sx * y;                                                     \
+        if (!FG(in[a])) continue;                                               \
+        if (EQV(in[a], in[a + sx - 1])) lab_unite(L, lab[a], lab[a + sx - 1]);  \
+        if (y > 0 && EQV(in[a], in[a - 1])) lab_unite(L, lab[a], lab[a - 1]);   \
+        if (y < sy - 1 && EQV(in[a], in[a + 2 * sx - 1]))                       \
+          lab_unite(L, lab[a], lab[a + 2 * sx - 1]);                            \
+      }                                                                         \
     }                                                                           \
   }                                                                             \
+  return L->n;                                                                  \
 }                                                                               \
 static int fg_##SUF(const void *in, int64_t i) { return FG(((const T *)in)[i]); } \
 /* Provisional labels the reference's binary labeller would create: a voxel  \
@@ -254,14 +296,6 @@ static void store_label(void *out, int out_dtype, int64_t i, uint64_t lab) {
   }
 }
 
-static uint64_t load_label(const void *out, int out_dtype, int64_t i) {
-  switch (out_dtype) {
-    case DT_U16: return ((const uint16_t *)out)[i];
-    case DT_U32: return ((const uint32_t *)out)[i];
-    default: return ((const uint64_t *)out)[i];
-  }
-}
-
 /* Estimated provisional label count and first/last foreground row
  * (cc3d/cc3d.hpp:287-315).  Returns (uint64_t)-1 on an unknown dtype. */
 uint64_t oracle_epl(const void *in, int dtype, int64_t sx, int64_t voxels,
@@ -321,14 +355,15 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     if (L > outmax) L = outmax;
     if (P >= L) return -5;
   }
-  uint32_t *par = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
-  if (!par) return -4;
+  uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+  if (!lab) return -4;
+  Labels L = {NULL, 0, 0, 0};
   int (*fg)(const void *, int64_t) = NULL;
   switch (dtype) {
 #define CASE(D, SUF, T)                                                     \
     case D:                                                                 \
-      unite_##SUF((const T *)in, sx, sy, sz, connectivity, binary,          \
-                  periodic, par);                                           \
+      first_pass_##SUF((const T *)in, sx, sy, sz, connectivity, binary,     \
+                       periodic, lab, &L);                                  \
       fg = fg_##SUF;                                                        \
       break;
     CASE(DT_U8, u8, uint8_t)
@@ -338,43 +373,43 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     CASE(DT_F32, f32, float)
     CASE(DT_F64, f64, double)
 #undef CASE
-    default: free(par); return -1;
+    default: free(lab); return -1;
   }
-  /* The parent of every non-root is smaller than the node itself (roots are
-     only ever linked under smaller roots), so one forward pass flattens every
-     tree: par[par[i]] is already the root when i is reached. */
-  for (int64_t i = 0; i < voxels; i++)
-    if (fg(in, i)) par[i] = par[par[i]];
+  if (L.oom) { free(lab); free(L.par); return -4; }
+  /* flatten: parents are smaller than children, so one increasing pass
+     leaves every label pointing at its root */
+  for (uint32_t p = 1; p <= L.n; p++) L.par[p] = L.par[L.par[p]];
+  uint32_t *ren = (uint32_t *)calloc((size_t)L.n + 1, sizeof(uint32_t));
+  if (!ren && L.n) { free(lab); free(L.par); return -4; }
   uint64_t n = 0;
   if (binary && connectivity == 8) {
     /* block-raster numbering: visit 2x2 blocks in raster order; a component
-       takes its number at the first block that holds one of its pixels.  The
-       number is parked at the root's own slot of `out`. */
-    for (int64_t i = 0; i < voxels; i++) store_label(out, out_dtype, i, 0);
+       takes its number at the first block that holds one of its pixels. */
     for (int64_t by = 0; by < sy; by += 2)
       for (int64_t bx = 0; bx < sx; bx += 2)
         for (int dy = 0; dy < 2; dy++)
           for (int dx = 0; dx < 2; dx++) {
             int64_t x = bx + dx, y = by + dy;
             if (x >= sx || y >= sy) continue;
-            int64_t i = x + sx * y;
-            if (!fg(in, i)) continue;
-            uint32_t r = par[i];
-            if (load_label(out, out_dtype, r) == 0) store_label(out, out_dtype, r, ++n);
+            uint32_t l = lab[x + sx * y];
+            if (!l) continue;
+            uint32_t r = L.par[l];
+            if (ren[r] == 0) ren[r] = (uint32_t)++n;
           }
-    for (int64_t i = 0; i < voxels; i++)
-      if (fg(in, i)) store_label(out, out_dtype, i, load_label(out, out_dtype, par[i]));
   } else {
-    /* raster numbering: the root of every tree is its minimum raster index,
-       i.e. the component's first voxel, so one forward pass numbers them. */
-    for (int64_t i = 0; i < voxels; i++) {
-      if (!fg(in, i)) { store_label(out, out_dtype, i, 0); continue; }
-      uint32_t r = par[i];
-      store_label(out, out_dtype, i,
-                  r == (uint32_t)i ? ++n : load_label(out, out_dtype, r));
-    }
+    /* the smallest provisional label of a component is the one its first
+       voxel opened, so numbering roots in label order is raster order */
+    for (uint32_t p = 1; p <= L.n; p++)
+      if (L.par[p] == p) ren[p] = (uint32_t)++n;
   }
-  free(par);
+  for (int64_t i = 0; i < voxels; i++) {
+    uint32_t l = lab[i];
+    store_label(out, out_dtype, i, l ? ren[L.par[l]] : 0);
+  }
+  (void)fg;
+  free(ren);
+  free(L.par);
+  free(lab);
   *N = n;
   return 0;
 }
