@@ -42,7 +42,7 @@ sys.path.insert(0, os.path.join(ROOT, "connected-components-3d_gb300"))
 import numpy as np  # noqa: E402
 
 METRIC = "GVoxels/s 512^3 uint32 26-conn labelling (bit-exact)"
-SHAPE = (512, 512, 512)
+SHAPE = (512, 512, 512)  # --size changes it for profiling captures only
 N_SEEDS = 4096
 LABEL_MAX = 1 << 20
 CONN = 26
@@ -234,35 +234,44 @@ def run_gpu(args, world, rank, local):
     ms_per_step = ms_total / args.steps
     value = world * voxels * args.steps / (ms_total / 1000.0) / 1e9
 
+    info = nat.Prepared()
+    sx, sy, sz = SHAPE[2], SHAPE[1], SHAPE[0]
+    nat.check(lib.cc3d_gpu_label_prepare(dev.data_ptr(), nat.U32, sx, sy, sz, CONN, 0, 0,
+                                         nat.IN_DEVICE | nat.OUT_DEVICE,
+                                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                         ctypes.byref(info)))
+    edges = int(info.edges)
+
     # ---------------- end to end through the C ABI with pinned host buffers
     pin_in = torch.from_numpy(vol).pin_memory()
     host_in = pin_in.numpy()
     osz = {torch.uint16: 2, torch.uint32: 4, torch.uint64: 8}[out_dtype]
     ocode = {2: nat.U16, 4: nat.U32, 8: nat.U64}[osz]
     pin_out = torch.empty(voxels * osz, dtype=torch.uint8).pin_memory()
-    sx, sy, sz = SHAPE[2], SHAPE[1], SHAPE[0]
 
     def e2e_step():
-        epl, first, last = ctypes.c_uint64(0), ctypes.c_int64(0), ctypes.c_int64(0)
-        nat.check(lib.cc3d_gpu_estimate_provisional_label_count(
-            host_in.ctypes.data, nat.U32, sx, voxels, ctypes.byref(epl), ctypes.byref(first),
-            ctypes.byref(last), 0, None))
+        # prepare (input staged once; the estimate comes from the same pass),
+        # then write the labels into the pinned host buffer
+        info = nat.Prepared()
+        nat.check(lib.cc3d_gpu_label_prepare(host_in.ctypes.data, nat.U32, sx, sy, sz, CONN, 0, 0, 0,
+                                             None, ctypes.byref(info)))
         n = ctypes.c_uint64(0)
-        nat.check(lib.cc3d_gpu_connected_components3d(
-            host_in.ctypes.data, nat.U32, sx, sy, sz, int(min(epl.value, voxels)), CONN, 0.0,
-            pin_out.data_ptr(), ocode, ctypes.byref(n), 0, 0, 0, None))
+        nat.check(lib.cc3d_gpu_label_finish(info.token, int(min(info.epl, voxels)), pin_out.data_ptr(),
+                                            ocode, ctypes.byref(n), 0, None))
         return n.value
 
-    for _ in range(args.warmup):
-        e2e_step()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        assert e2e_step() == N
-    t_e2e = max_over_ranks(world, time.perf_counter() - t0)
-    e2e_value = world * voxels * args.steps / t_e2e / 1e9
-    expect = out.cpu().numpy().reshape(-1).view(np.uint8)
-    assert np.array_equal(pin_out.numpy(), expect), "e2e labels differ from the device path"
+    e2e_value = None
+    if not args.skip_e2e:
+        for _ in range(args.warmup):
+            e2e_step()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            assert e2e_step() == N
+        t_e2e = max_over_ranks(world, time.perf_counter() - t0)
+        e2e_value = world * voxels * args.steps / t_e2e / 1e9
+        expect = out.cpu().numpy().reshape(-1).view(np.uint8)
+        assert np.array_equal(pin_out.numpy(), expect), "e2e labels differ from the device path"
 
     # ---------------- roofline of the dominant kernel
     peak, peak_kind = load_peaks()
@@ -272,10 +281,9 @@ def run_gpu(args, world, rank, local):
         # traffic the kernel is responsible for
         "tile_local": voxels * isz,
         "write": voxels * osz_b,
-        "epl": voxels * isz,
     }
     per_launch = {k: (stage[k][0] / stage[k][1] if stage[k][1] else 0.0) for k in stage}
-    dom = max(("tile_local", "write", "epl"), key=lambda k: per_launch[k])
+    dom = max(("tile_local", "write"), key=lambda k: per_launch[k])
     dom_ms = per_launch[dom]
     achieved = kern_bytes[dom] / (dom_ms / 1000.0) / 1e9 if dom_ms else 0.0
     job_bytes = voxels * (isz + osz_b)
@@ -290,7 +298,7 @@ def run_gpu(args, world, rank, local):
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_reference(vol)
 
-    launches_per_step = 7  # epl, tile_local, merge_edges, 3 scan kernels, write
+    launches_per_step = 8  # tile pass, edge merge, 3 scan kernels + tile reduction, resolve, write
     line = {
         "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -298,11 +306,11 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic (seeded Voronoi; the reference publishes no number for this config)",
         "config": {"workload": "512^3 uint32 Voronoi(4096 seeds, labels in [1,2^20])+membrane+2% salt, "
                                "connectivity 26, output uint32",
-                   "volumes_per_step_per_gpu": 1, "N": N,
+                   "volumes_per_step_per_gpu": 1, "N": N, "boundary_edges": edges,
                    "l2": "input (512 MiB) larger than L2, no flush"},
         "e2e": {"value": e2e_value, "unit": "GVoxels/s",
-                "h2d_bytes_per_step": 2 * voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
-                "path": "C ABI, pinned host buffers, epl call + label call (input staged by each)"},
+                "h2d_bytes_per_step": voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
+                "path": "C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish), pinned host buffers"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": kern_bytes[dom], "avg_launch_ms": dom_ms},
@@ -325,7 +333,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--size", type=int, default=512, help="cube edge (profiling captures only)")
     args = ap.parse_args()
+    global SHAPE, N_SEEDS
+    if args.size != 512:
+        SHAPE = (args.size,) * 3
+        N_SEEDS = max(1, 4096 * args.size ** 3 // 512 ** 3)
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()

@@ -29,6 +29,8 @@ EXPORTED = (
     "cc3d_gpu_version",
     "cc3d_gpu_estimate_provisional_label_count",
     "cc3d_gpu_connected_components3d",
+    "cc3d_gpu_label_prepare",
+    "cc3d_gpu_label_finish",
     "cc3d_gpu_special_row",
     "cc3d_gpu_label_minmax",
     "cc3d_gpu_statistics",
@@ -37,6 +39,13 @@ EXPORTED = (
     "cc3d_gpu_release_workspace",
 )
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
+
+class Prepared(ctypes.Structure):
+    """cc3d_gpu_prepared (include/cc3d_gpu.h)."""
+    _fields_ = [("token", ctypes.c_uint64), ("epl", ctypes.c_uint64), ("first_row", ctypes.c_int64),
+                ("last_row", ctypes.c_int64), ("N", ctypes.c_uint64), ("provisional", ctypes.c_uint64),
+                ("edges", ctypes.c_uint64)]
+
 
 _lock = threading.Lock()
 _lib = None
@@ -67,6 +76,9 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_estimate_provisional_label_count.argtypes = [vp, ci, i64, i64, u64p, i64p, i64p, ci, vp]
         lib.cc3d_gpu_connected_components3d.argtypes = [
             vp, ci, i64, i64, i64, i64, i64, ctypes.c_double, vp, ci, u64p, ci, ci, ci, vp]
+        lib.cc3d_gpu_label_prepare.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, ci, vp,
+                                               ctypes.POINTER(Prepared)]
+        lib.cc3d_gpu_label_finish.argtypes = [ctypes.c_uint64, i64, vp, ci, u64p, ci, vp]
         lib.cc3d_gpu_special_row.argtypes = [vp, ci, ci, i64, i64, i64, i64, vp, ci, u64p, ci, vp]
         lib.cc3d_gpu_label_minmax.argtypes = [vp, ci, ci, i64, u64p, i64p, ci, vp]
         lib.cc3d_gpu_statistics.argtypes = [vp, ci, i64, i64, i64, ci, ci, ctypes.c_uint64, vp, vp, ci, vp, ci, vp]
@@ -74,7 +86,7 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_profile_enable.argtypes = [ci]
         lib.cc3d_gpu_profile_enable.restype = None
         lib.cc3d_gpu_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), u64p, ci]
-        for name in EXPORTED[2:7] + ("cc3d_gpu_profile_read",):
+        for name in EXPORTED[2:9] + ("cc3d_gpu_profile_read",):
             getattr(lib, name).restype = ctypes.c_int
         _lib = lib
         return lib

@@ -261,10 +261,21 @@ def connected_components(
     sx, sy, sz = (int(v) for v in shape)
     voxels = sx * sy * sz
 
-    if dtype not in _CODE and not (binary_image or dtype == bool):
+    if np.dtype(dtype) not in _CODE:
         raise TypeError(_UNSUPPORTED.format(dtype))
-    binary_image = bool(binary_image or (dtype == bool))
-    code = _CODE.get(np.dtype(dtype))
+    code = _CODE[np.dtype(dtype)]
+    binary0 = bool(binary_image or (dtype == bool))
+    # delta equal to the dtype's maximum makes any image binary (fastcc3d.pyx:397-403)
+    if np.issubdtype(dtype, np.floating):
+        delta = float(delta)
+        binary_image = binary0 or (delta == np.finfo(dtype).max)
+    else:
+        delta = int(delta)
+        binary_image = binary0 or (delta == np.iinfo(dtype).max)
+    if delta != 0 and not binary_image:
+        raise NotImplementedError(
+            "continuous-value labelling (delta != 0) is not implemented on the GPU path")
+
     if on_device:
         stream = dev.stream()
         torch = _torch()
@@ -272,26 +283,35 @@ def connected_components(
         ptr = t.data_ptr()
     else:
         stream = None
+        devctx = None
         flat = _reshape_flat(data)
         ptr = flat.ctypes.data
     mem_in = nat.IN_DEVICE if on_device else 0
+    mem_out_hint = nat.OUT_DEVICE if (on_device and out_file is None) else 0
+    lib = nat.load()
 
-    if binary_image:
-        epl, first_row, last_row = voxels, 0, sy
-    else:
-        if on_device:
+    def call(fn, *args):
+        if devctx is not None:
             with devctx:
-                epl, first_row, last_row = _epl_call(ptr, code, sx, voxels, mem_in, stream)
-        else:
-            epl, first_row, last_row = _epl_call(ptr, code, sx, voxels, mem_in, stream)
-    max_labels = min(epl, voxels)
+                return fn(*args)
+        return fn(*args)
 
-    if np.issubdtype(dtype, np.floating):
-        delta = float(delta)
-        binary_image = binary_image or (delta == np.finfo(dtype).max)
+    # labelling up to the numbering; the same pass computes the estimate
+    info = nat.Prepared()
+    nat.check(call(lib.cc3d_gpu_label_prepare, ptr, code, sx, sy, sz, int(connectivity),
+                   int(bool(periodic_boundary)), int(binary_image), mem_in | mem_out_hint, stream,
+                   ctypes.byref(info)))
+    if binary0:
+        epl, first_row, last_row = voxels, 0, sy
+    elif binary_image:
+        epl, first_row, last_row = call(_epl_call, ptr, code, sx, voxels, mem_in, stream)
+        info = nat.Prepared()
+        nat.check(call(lib.cc3d_gpu_label_prepare, ptr, code, sx, sy, sz, int(connectivity),
+                       int(bool(periodic_boundary)), 1, mem_in | mem_out_hint, stream,
+                       ctypes.byref(info)))
     else:
-        delta = int(delta)
-        binary_image = binary_image or (delta == np.iinfo(dtype).max)
+        epl, first_row, last_row = int(info.epl), int(info.first_row), int(info.last_row)
+    max_labels = min(epl, voxels)
 
     ufv = _even_ceil(padded_shape[0]) * _even_ceil(padded_shape[1]) * _even_ceil(padded_shape[2])
     if binary_image:
@@ -320,8 +340,6 @@ def connected_components(
         out_dtype = np.dtype(np.uint64)
 
     special = (delta == 0 and first_row == last_row and first_row >= 0)
-    if code is None:
-        raise TypeError(_UNSUPPORTED.format(dtype))
 
     # output buffer: host (numpy / memmap) or device (torch)
     if out_file is not None:
@@ -340,28 +358,16 @@ def connected_components(
         out = np.zeros((voxels,), dtype=out_dtype, order="F")
         out_ptr, mem_out = out.ctypes.data, 0
 
-    lib = nat.load()
     n = ctypes.c_uint64(0)
-    mem = mem_in | mem_out
     ocode = _OUT_CODE[out_dtype]
-
-    def run():
-        if special:
-            is_u64 = int(np.dtype(dtype) == np.uint64)
-            nat.check(lib.cc3d_gpu_special_row(ptr, code, is_u64, sx, sy, sz, int(first_row),
-                                               out_ptr, ocode, ctypes.byref(n), mem, stream))
-        else:
-            if delta != 0 and not binary_image:
-                raise NotImplementedError("continuous-value labelling (delta != 0) is not implemented on the GPU path")
-            nat.check(lib.cc3d_gpu_connected_components3d(
-                ptr, code, sx, sy, sz, int(max_labels), int(connectivity), float(delta) if not binary_image else 0.0,
-                out_ptr, ocode, ctypes.byref(n), int(bool(periodic_boundary)), int(binary_image), mem, stream))
-
-    if on_device:
-        with devctx:
-            run()
+    if special:
+        # the Cython layer's single-row loop (fastcc3d.pyx:469-470, 644-679)
+        is_u64 = int(np.dtype(dtype) == np.uint64)
+        nat.check(call(lib.cc3d_gpu_special_row, ptr, code, is_u64, sx, sy, sz, int(first_row),
+                       out_ptr, ocode, ctypes.byref(n), mem_in | mem_out, stream))
     else:
-        run()
+        nat.check(call(lib.cc3d_gpu_label_finish, info.token, int(max_labels), out_ptr, ocode,
+                       ctypes.byref(n), mem_out, stream))
     N = int(n.value)
 
     out = _final_reshape(out, sx, sy, sz, dims, order)

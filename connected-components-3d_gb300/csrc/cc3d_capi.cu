@@ -54,8 +54,27 @@ struct Profile {
 };
 thread_local Profile g_prof;
 
+// the labelling prepared by cc3d_gpu_label_prepare, finished by
+// cc3d_gpu_label_finish on the same thread
+struct Job {
+  uint64_t token = 0;
+  bool empty = false;
+  bool ready = false;
+  bool binary = false;
+  int conn = 0;
+  int64_t voxels = 0;
+  int64_t ntiles = 0;
+  uint64_t N = 0;
+  uint64_t prov = 0;
+  size_t out_staging_offset = 0;
+  LabelArgs args;
+};
+
 struct Workspace {
   cudaEvent_t ev[CC3D_PROFILE_STAGES + 1] = {};
+  Job job;
+  uint64_t next_token = 0;
+  void* spill = nullptr;
   void* dev = nullptr;
   size_t size = 0;
   Counters* host_ctr = nullptr;
@@ -65,6 +84,18 @@ struct Workspace {
 
 // one workspace per (thread, device); released explicitly or at process exit
 thread_local std::map<int, Workspace> g_ws;
+
+int get_ws(Workspace*& out);
+
+// entry points other than label_finish reuse the arena: forget a prepared job
+int get_ws_fresh(Workspace*& out) {
+  int rc = get_ws(out);
+  if (rc == CC3D_OK) {
+    out->job.ready = false;
+    out->job.token = 0;
+  }
+  return rc;
+}
 
 int get_ws(Workspace*& out) {
   int dev = 0;
@@ -82,6 +113,7 @@ int get_ws(Workspace*& out) {
 
 int reserve(Workspace& w, size_t bytes) {
   if (bytes <= w.size) return CC3D_OK;
+  w.job.ready = false;  // a prepared labelling lived in the old arena
   if (w.dev) {
     cudaFree(w.dev);
     w.dev = nullptr;
@@ -121,11 +153,12 @@ cudaStream_t pick_stream(Workspace& w, void* stream, int mem_flags) {
 int check_device_errors(unsigned err) {
   if (!err) return CC3D_OK;
   return fail(CC3D_ERR_DEVICE,
-              "device kernel gave up (error bits 0x%x: %s%s%s%s)", err,
+              "device kernel gave up (error bits 0x%x: %s%s%s%s%s)", err,
               (err & ERR_UNITE_BUDGET) ? "union budget " : "",
               (err & ERR_FIND_BUDGET) ? "find budget " : "",
               (err & ERR_EDGE_OVERFLOW) ? "edge buffer overflow " : "",
-              (err & ERR_LOCAL_BUDGET) ? "tile union budget" : "");
+              (err & ERR_LOCAL_BUDGET) ? "tile union budget " : "",
+              (err & ERR_INDEX) ? "index range check" : "");
 }
 
 Counters fresh_counters() {
@@ -227,7 +260,7 @@ int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t
     return CC3D_OK;
   }
   Workspace* w;
-  if (int rc = get_ws(w)) return rc;
+  if (int rc = get_ws_fresh(w)) return rc;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);
   Carver cv;
   const size_t o_ctr = cv.take(sizeof(Counters));
@@ -256,42 +289,37 @@ int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t
   return CC3D_OK;
 }
 
-int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
-                                    int64_t max_labels, int64_t connectivity, double delta,
-                                    void* out, int out_dtype, uint64_t* N, int periodic_boundary,
-                                    int binary_image, int mem_flags, void* stream) {
+int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                           int64_t connectivity, int periodic_boundary, int binary_image,
+                           int mem_flags, void* stream, cc3d_gpu_prepared* info) {
   const size_t isz = dtype_size(dtype);
   if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
-  if (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64)
-    return fail(CC3D_ERR_INVALID, "out_dtype must be uint16, uint32 or uint64 (code %d)", out_dtype);
-  const size_t osz = dtype_size(out_dtype);
-  if (sx < 0 || sy < 0 || sz < 0 || !N) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  if (sx < 0 || sy < 0 || sz < 0 || !info) return fail(CC3D_ERR_INVALID, "invalid arguments");
   const int conn = (int)connectivity;
   if (conn != 26 && conn != 18 && conn != 6 && conn != 8 && conn != 4)
     return fail(CC3D_ERR_RUNTIME, "Only 4 and 8 2D and 6, 18, and 26 3D connectivities are supported.");
   if ((conn == 8 || conn == 4) && sz != 1)
     return fail(CC3D_ERR_RUNTIME, "sz must be 1 for 2D connectivities.");
-  if (delta != 0.0 && !binary_image)
-    return fail(CC3D_ERR_UNSUPPORTED, "continuous-value labelling (delta != 0) is not implemented");
   if (periodic_boundary && conn != 4 && conn != 8 && conn != 6)
     return fail(CC3D_ERR_INVALID, "periodic_boundary is only implemented for 4, 8 and 6 connectivity");
-  *N = 0;
+  memset(info, 0, sizeof(*info));
+  info->first_row = -1;
+  info->last_row = -1;
   const int64_t voxels = sx * sy * sz;
-  if (voxels == 0) return CC3D_OK;
-
   Workspace* w;
   if (int rc = get_ws(w)) return rc;
-  cudaStream_t s = pick_stream(*w, stream, mem_flags);
-
-  if (max_labels == 0) {  // the reference returns before labelling
-    if (mem_flags & CC3D_OUT_DEVICE) {
-      CK(cudaMemsetAsync(out, 0, voxels * osz, s));
-      CK(cudaStreamSynchronize(s));
-    } else {
-      memset(out, 0, voxels * osz);
-    }
+  Job& job = w->job;
+  job = Job();
+  job.token = ++w->next_token;
+  info->token = job.token;
+  job.voxels = voxels;
+  job.conn = conn;
+  job.binary = binary_image != 0;
+  if (voxels == 0) {
+    job.empty = true;
     return CC3D_OK;
   }
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
 
   // effective neighbourhood: a single z plane makes 26/18 equal to 8 and 6 to 4
   int eff = conn;
@@ -302,7 +330,7 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
   const bool d3 = (eff == 26 || eff == 18 || eff == 6);
   const int TY = d3 ? 8 : 64, TZ = d3 ? 8 : 1, HZ = d3 ? 1 : 0;
 
-  LabelArgs a;
+  LabelArgs& a = job.args;
   memset(&a, 0, sizeof(a));
   a.sx = sx; a.sy = sy; a.sz = sz;
   a.ntx = (int)((sx + kTX - 1) / kTX);
@@ -326,33 +354,40 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
   }
   if (nwords * 32 >= 0xFFFFFFFFLL)
     return fail(CC3D_ERR_UNSUPPORTED, "volume too large for 32-bit component keys");
-  const int64_t halo = (int64_t)(kTX + 2) * (TY + 2) * (TZ + HZ) - kTV;
-  const int64_t edge_cap64 = ntiles * halo;
-  a.edge_cap = (unsigned)(edge_cap64 > 0xFFFFFFF0LL ? 0xFFFFFFF0LL : edge_cap64);
-  a.want_epl = 0;
+  a.nwords = nwords;
+  // at most one edge per halo run head or halo column voxel
+  a.edge_slots = (unsigned)((TY + 2) * (TZ + HZ) * 34 - kTV);
+  a.ntiles = ntiles;
+  a.want_epl = binary_image ? 0 : 1;
   a.want_prov = binary_image ? 1 : 0;
 
   const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);
-  const bool stage_out = !(mem_flags & CC3D_OUT_DEVICE);
   const int64_t nblocks = scan_blocks_needed(nwords);
   Carver cv;
   const size_t o_ctr = cv.take(sizeof(Counters));
   const size_t o_in = stage_in ? cv.take(voxels * isz) : 0;
-  const size_t o_out = stage_out ? cv.take(voxels * osz) : 0;
-  const size_t o_rec = cv.take(ntiles * kTV * sizeof(uint16_t));
+  const size_t o_rm = cv.take(ntiles * kRowsPerTile * sizeof(uint2));
+  const size_t o_rr = cv.take(ntiles * kRowsPerTile * sizeof(uint16_t));
+  const size_t o_rc = cv.take(ntiles * kTV * sizeof(uint16_t));
   const size_t o_E = cv.take(ntiles * kTV * sizeof(unsigned long long));
-  const size_t o_cc = cv.take(ntiles * sizeof(uint32_t));
+  const size_t o_L = cv.take(ntiles * kTV * sizeof(uint32_t));
+  const size_t o_cc = cv.take(ntiles * sizeof(TileInfo));
   const size_t o_bm = cv.take(nwords * sizeof(uint32_t));
   const size_t o_pf = cv.take(nwords * sizeof(uint32_t));
   const size_t o_bs = cv.take((nblocks + 1) * sizeof(uint32_t));
-  const size_t o_ed = cv.take((size_t)a.edge_cap * sizeof(uint2));
+  const size_t o_ed = cv.take((size_t)ntiles * a.edge_slots * sizeof(uint2));
+  // host outputs are staged after the job's buffers (room for uint64 labels)
+  job.out_staging_offset = cv.take((mem_flags & CC3D_OUT_DEVICE) ? 0 : voxels * 8);
   if (int rc = reserve(*w, cv.off)) return rc;
   char* base = (char*)w->dev;
   Counters* ctr = (Counters*)(base + o_ctr);
   a.ctr = ctr;
-  a.rec = (uint16_t*)(base + o_rec);
+  a.rmask = (uint2*)(base + o_rm);
+  a.rrow = (uint16_t*)(base + o_rr);
+  a.rcomp = (uint16_t*)(base + o_rc);
   a.E = (unsigned long long*)(base + o_E);
-  a.ccount = (uint32_t*)(base + o_cc);
+  a.label = (uint32_t*)(base + o_L);
+  a.tinfo = (TileInfo*)(base + o_cc);
   a.bitmap = (uint32_t*)(base + o_bm);
   a.prefix = (uint32_t*)(base + o_pf);
   a.edges = (uint2*)(base + o_ed);
@@ -368,8 +403,6 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
     a.in = base + o_in;
     tm.mark(0);
   }
-  void* dout = stage_out ? (void*)(base + o_out) : out;
-
   CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, ntiles, s));
   tm.mark(2);
   CK(launch_merge_edges(a, s));
@@ -380,23 +413,61 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
   }
   CK(launch_scan(a, nwords, bsum, nblocks, s));
   tm.mark(5);
-  CK(launch_write(a, dout, out_dtype, ntiles, s));
-  tm.mark(6);
-  if (stage_out) {
-    CK(cudaMemcpyAsync(out, dout, voxels * osz, cudaMemcpyDeviceToHost, s));
-    tm.mark(7);
-  }
   CK(cudaMemcpyAsync(w->host_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   tm.finish();
   const Counters& h = *w->host_ctr;
   if (int rc = check_device_errors(h.err)) return rc;
+  job.ntiles = ntiles;
+  job.ready = true;
+  job.N = h.N;
+  job.prov = h.prov;
+  info->N = h.N;
+  info->provisional = h.prov;
+  info->edges = h.edges;
   if (binary_image) {
+    info->epl = (uint64_t)voxels;
+    info->first_row = 0;
+    info->last_row = sy;
+  } else {
+    info->epl = h.epl;
+    info->first_row = h.epl ? h.first_row : -1;
+    info->last_row = h.epl ? h.last_row : -1;
+  }
+  return CC3D_OK;
+}
+
+int cc3d_gpu_label_finish(uint64_t token, int64_t max_labels, void* out, int out_dtype, uint64_t* N,
+                          int mem_flags, void* stream) {
+  if (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64)
+    return fail(CC3D_ERR_INVALID, "out_dtype must be uint16, uint32 or uint64 (code %d)", out_dtype);
+  if (!N) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  Workspace* w;
+  if (int rc = get_ws(w)) return rc;
+  Job& job = w->job;
+  if (job.token != token || token == 0)
+    return fail(CC3D_ERR_INVALID, "no prepared labelling with this token on this thread");
+  *N = 0;
+  if (job.empty) return CC3D_OK;
+  if (!job.ready) return fail(CC3D_ERR_INVALID, "the prepared labelling did not complete");
+  const size_t osz = dtype_size(out_dtype);
+  const int64_t voxels = job.voxels;
+  cudaStream_t s = pick_stream(*w, stream, mem_flags);
+  if (max_labels == 0) {  // the reference returns before labelling
+    if (mem_flags & CC3D_OUT_DEVICE) {
+      CK(cudaMemsetAsync(out, 0, voxels * osz, s));
+      CK(cudaStreamSynchronize(s));
+    } else {
+      memset(out, 0, voxels * osz);
+    }
+    return CC3D_OK;
+  }
+  if (job.binary) {
     // the reference's binary labellers size their union-find from max_labels
     // with per-labeller caps and throw when a provisional label reaches it
     const uint64_t V = (uint64_t)voxels;
     uint64_t L = (uint64_t)max_labels + 1;
-    switch (conn) {
+    switch (job.conn) {
       case 26: L = (L < (V >> 2) + 1 ? L : (V >> 2) + 1) + 1; break;
       case 18: L = (L < V + 1 ? L : V + 1); break;
       case 8: L = (L < (V >> 1) + 1 ? L : (V >> 1) + 1); if (L < 1) L = 1; L += 1; break;
@@ -404,10 +475,56 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
     }
     const uint64_t outmax = out_dtype == CC3D_U16 ? 0xFFFFull : out_dtype == CC3D_U32 ? 0xFFFFFFFFull : ~0ull;
     if (L > outmax) L = outmax;
-    if (h.prov >= L) return fail(CC3D_ERR_RUNTIME, "maximum length exception");
+    if (job.prov >= L) return fail(CC3D_ERR_RUNTIME, "maximum length exception");
   }
-  *N = h.N;
+  const bool stage_out = !(mem_flags & CC3D_OUT_DEVICE);
+  void* dout = out;
+  if (stage_out) {
+    // grow the arena past the job's buffers without moving them
+    const size_t need = job.out_staging_offset + voxels * osz;
+    if (need > w->size) {
+      void* extra = nullptr;
+      CK(cudaMalloc(&extra, voxels * osz));
+      w->spill = extra;
+      dout = extra;
+    } else {
+      dout = (char*)w->dev + job.out_staging_offset;
+    }
+  }
+  StageTimer tm(*w, s);
+  CK(launch_write(job.args, dout, out_dtype, job.ntiles, s));
+  tm.mark(6);
+  if (stage_out) {
+    CK(cudaMemcpyAsync(out, dout, voxels * osz, cudaMemcpyDeviceToHost, s));
+    tm.mark(7);
+  }
+  CK(cudaMemcpyAsync(w->host_ctr, job.args.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  tm.finish();
+  if (w->spill) {
+    cudaFree(w->spill);
+    w->spill = nullptr;
+  }
+  if (int rc = check_device_errors(w->host_ctr->err)) return rc;
+  *N = job.N;
   return CC3D_OK;
+}
+
+int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                                    int64_t max_labels, int64_t connectivity, double delta,
+                                    void* out, int out_dtype, uint64_t* N, int periodic_boundary,
+                                    int binary_image, int mem_flags, void* stream) {
+  if (!N) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  if (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64)
+    return fail(CC3D_ERR_INVALID, "out_dtype must be uint16, uint32 or uint64 (code %d)", out_dtype);
+  if (delta != 0.0 && !binary_image)
+    return fail(CC3D_ERR_UNSUPPORTED, "continuous-value labelling (delta != 0) is not implemented");
+  cc3d_gpu_prepared info;
+  if (int rc = cc3d_gpu_label_prepare(in, dtype, sx, sy, sz, connectivity, periodic_boundary,
+                                      binary_image, mem_flags, stream, &info))
+    return rc;
+  return cc3d_gpu_label_finish(info.token, max_labels, out, out_dtype, N, mem_flags & CC3D_OUT_DEVICE,
+                               stream);
 }
 
 int cc3d_gpu_special_row(const void* in, int dtype, int is_uint64, int64_t sx, int64_t sy, int64_t sz,
@@ -418,7 +535,7 @@ int cc3d_gpu_special_row(const void* in, int dtype, int is_uint64, int64_t sx, i
     return fail(CC3D_ERR_INVALID, "invalid arguments");
   if (row < 0 || row >= sy * sz) return fail(CC3D_ERR_INVALID, "row %lld out of range", (long long)row);
   Workspace* w;
-  if (int rc = get_ws(w)) return rc;
+  if (int rc = get_ws_fresh(w)) return rc;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);
   const bool stage_in = !(mem_flags & CC3D_IN_DEVICE), stage_out = !(mem_flags & CC3D_OUT_DEVICE);
   Carver cv;
@@ -459,7 +576,7 @@ int cc3d_gpu_label_minmax(const void* labels, int dtype, int is_signed, int64_t 
   if (!isz || dtype == CC3D_F32 || dtype == CC3D_F64 || !vmax || !vmin || voxels <= 0)
     return fail(CC3D_ERR_INVALID, "invalid arguments");
   Workspace* w;
-  if (int rc = get_ws(w)) return rc;
+  if (int rc = get_ws_fresh(w)) return rc;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);
   const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);
   Carver cv;
@@ -493,7 +610,7 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   const int64_t voxels = d0 * d1 * d2;
   if (N > (uint64_t)voxels) return fail(CC3D_ERR_INVALID, "N exceeds the voxel count");
   Workspace* w;
-  if (int rc = get_ws(w)) return rc;
+  if (int rc = get_ws_fresh(w)) return rc;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);
   const int64_t n1 = (int64_t)N + 1;
   const bool stage_in = !(mem_flags & CC3D_IN_DEVICE), stage_out = !(mem_flags & CC3D_OUT_DEVICE);

@@ -7,14 +7,24 @@ namespace cc3dgpu {
 // ------------------------------------------------------- K2: edge merges
 // Every edge joins a tile component (x = its node) with the component that
 // owns a halo voxel in the neighbouring tile (y = tile * 2048 + voxel index).
+// One warp per tile walks the tile's edge slots.
 __global__ void __launch_bounds__(256) k_merge_edges(LabelArgs p) {
-  unsigned n = *(volatile unsigned*)&p.ctr->edge_count;
-  if (n > p.edge_cap) n = p.edge_cap;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint2 e = p.edges[i];
-    const uint32_t otile = e.y / kTV;
-    const uint16_t c = p.rec[e.y];
-    gunite(p.E, e.x, otile * kTV + c, p.bitmap, p.ctr);
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < p.ntiles;
+       tile += warps) {
+    const uint32_t n = p.tinfo[tile].nedges;
+    const uint2* edges = p.edges + tile * p.edge_slots;
+    for (uint32_t i = lane; i < n; i += 32) {
+      const uint2 e = edges[i];
+      const uint32_t otile = e.y / kTV, local = e.y % kTV;
+      if (e.x >= (uint64_t)p.ntiles * kTV) {
+        atomicOr(&p.ctr->err, ERR_INDEX);
+        continue;
+      }
+      gunite(p.E, e.x, record_node(p, otile, (int)(local >> 5), (int)(local & 31)), p.bitmap, p.nwords,
+             p.ctr);
+    }
   }
 }
 
@@ -81,6 +91,44 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t* bsum, int64_t nb
   if (threadIdx.x == 0) ctr->N = carry;
 }
 
+// reduction of the tile pass's per-tile results (one block)
+__global__ void __launch_bounds__(1024) k_reduce_tiles(const TileInfo* ti, int64_t ntiles, Counters* ctr) {
+  unsigned long long epl = 0, prov = 0, edges = 0;
+  long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+  for (int64_t t = threadIdx.x; t < ntiles; t += blockDim.x) {
+    const TileInfo x = ti[t];
+    epl += x.epl;
+    prov += x.prov;
+    edges += x.nedges;
+    f = x.first_row < f ? x.first_row : f;
+    l = x.last_row > l ? x.last_row : l;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    epl += __shfl_down_sync(FULL, epl, o);
+    prov += __shfl_down_sync(FULL, prov, o);
+    edges += __shfl_down_sync(FULL, edges, o);
+    f = min(f, (long long)__shfl_down_sync(FULL, f, o));
+    l = max(l, (long long)__shfl_down_sync(FULL, l, o));
+  }
+  __shared__ unsigned long long se[32], sp[32], sd[32];
+  __shared__ long long sf[32], sl[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { se[warp] = epl; sp[warp] = prov; sd[warp] = edges; sf[warp] = f; sl[warp] = l; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      epl += se[w]; prov += sp[w]; edges += sd[w];
+      f = sf[w] < f ? sf[w] : f;
+      l = sl[w] > l ? sl[w] : l;
+    }
+    ctr->epl = epl;
+    ctr->prov = prov;
+    ctr->edges = (unsigned)(edges > 0xFFFFFFFFull ? 0xFFFFFFFFull : edges);
+    ctr->first_row = f;
+    ctr->last_row = l;
+  }
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(const uint32_t* bitmap, int64_t nwords,
                                                             const uint32_t* bsum, uint32_t* prefix) {
   __shared__ uint32_t ws[kScanThreads / 32];
@@ -108,13 +156,42 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
   if (nblocks == 0) return cudaSuccess;
   k_scan_reduce<<<(unsigned)nblocks, kScanThreads, 0, s>>>(a.bitmap, nwords, bsum);
   k_scan_blocks<<<1, 1024, 0, s>>>(bsum, nblocks, a.ctr);
+  k_reduce_tiles<<<1, 1024, 0, s>>>(a.tinfo, a.ntiles, a.ctr);
   k_scan_down<<<(unsigned)nblocks, kScanThreads, 0, s>>>(a.bitmap, nwords, bsum, a.prefix);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- resolve
+// Final label of every component: 1 + rank of its root's key among the
+// surviving keys.  One warp per tile, one lane per component.
+__global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < p.ntiles;
+       tile += warps) {
+    uint32_t C = p.tinfo[tile].C;
+    if (C > kTV) C = kTV;
+    const uint32_t node0 = (uint32_t)(tile * kTV);
+    for (uint32_t c = lane; c < C; c += 32) {
+      const uint32_t R = gfind(p.E, node0 + c, p.ctr);
+      const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
+      const uint32_t w = key >> 5;
+      uint32_t lab = 0;
+      if (w < p.nwords) {
+        const uint32_t below = __ldg(p.bitmap + w) & ((1u << (key & 31)) - 1u);
+        lab = __ldg(p.prefix + w) + __popc(below) + 1u;
+      } else {
+        atomicOr(&p.ctr->err, ERR_INDEX);
+      }
+      p.label[node0 + c] = lab;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- writer
 template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
+  k_resolve<<<152 * 16, 256, 0, s>>>(a);
   if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
   else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
   else return cudaErrorInvalidValue;

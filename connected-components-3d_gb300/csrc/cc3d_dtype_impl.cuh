@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) k_minmax(const T* in, int64_t n, int is_s
 // ------------------------------------------------------------- launchers
 template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
 cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  k_tile_local<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  k_tile_runs<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "cc3d_label.cuh"
+#include "cc3d_tile.cuh"
 
 namespace cc3dgpu {
 

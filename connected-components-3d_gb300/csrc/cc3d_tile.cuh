@@ -1,0 +1,621 @@
+// cc3d_tile.cuh -- the tile pass (K1) of the labelling pipeline.
+//
+// One CTA labels one 32 x TY x TZ tile (2048 voxels) with a one-voxel backward
+// halo, all in shared memory:
+//
+//   phase 0  rows of 32 values are loaded (one warp per row, 128 B coalesced
+//            for uint32) with the two halo columns; foreground and run-start
+//            masks come from warp ballots, and the provisional-label estimate
+//            (cc3d/cc3d.hpp:287-315) is counted on the tile's own rows.
+//   phase 2  every tile row is related to its backward rows.  Equalities at
+//            dx = 0 are one ballot per neighbour row; a union is queued only
+//            where a pair of overlapping runs starts.  Where the connectivity
+//            allows it, a voxel equal to its "primary" neighbour (the voxel
+//            below for 26, below and behind for 18, the row behind for 8)
+//            needs nothing else: each of its other backward neighbours that it
+//            relates to is also a neighbour of the primary one, related to it,
+//            and earlier in raster order, so that pair is joined by induction
+//            over the raster order.  Only the remaining voxels are queued as
+//            "items" that test their dx = +-1 neighbours and the halo columns.
+//            Unions and items go through small per-warp queues and are run in
+//            dense rounds (lane i takes entry i).  Halo rows are grouped with
+//            same-owner halo rows in a second forest.
+//   phase 3  roots -> dense component ids in tile raster order, run-length
+//            records, component keys, the numbering bitmap, one edge per
+//            (component, halo group), the binary labellers' provisional count.
+#pragma once
+
+#include "cc3d_label.cuh"
+
+namespace cc3dgpu {
+
+// Box geometry of a 32 x TY x TZ tile with its backward halo: rows rb =
+// bz * BY + by; tile rows have by in [1, TY] and bz >= HZ.  Union-find nodes:
+// tile run heads ri * 32 + x, halo run heads kTV + rb * 32 + x, halo columns
+// CNODE + rb (x0 - 1) and CNODE + NRB + rb (x0 + 32).
+template <int CONN, int TY, int TZ>
+struct TileBox {
+  static constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
+  static constexpr int HZ = D3 ? 1 : 0;
+  static constexpr int BY = TY + 2, BZ = TZ + HZ;
+  static constexpr int NRB = BY * BZ;
+  static constexpr int HNODE = kTV;
+  static constexpr int CNODE = kTV + NRB * 32;
+  static constexpr int NODES = CNODE + 2 * NRB;
+  __device__ static __forceinline__ bool is_tile_row(int rb) {
+    const int by = rb % BY, bz = rb / BY;
+    return by >= 1 && by <= TY && bz >= HZ;
+  }
+  __device__ static __forceinline__ unsigned node_of(int rb, int h) {
+    return is_tile_row(rb) ? (unsigned)(((rb % BY - 1) + TY * (rb / BY - HZ)) * 32 + h)
+                           : (unsigned)(HNODE + rb * 32 + h);
+  }
+};
+
+// One queued item of the tile pass: voxel x of box row rb, not covered by its
+// primary neighbour, tests its dx = +-1 neighbours and the halo columns.
+// Not inlined, so that its unions share one copy of the union-find code.
+// Returns a nonzero error code if a union ran out of budget.
+template <typename S, int CONN, int TY, int TZ, int MODE>
+__device__ __noinline__ int tile_item(int it, const S* sv, const S* scol0, const S* scol1,
+                                      const uint32_t* smask, unsigned short* par) {
+  using B = TileBox<CONN, TY, TZ>;
+  const int rb = it >> 5, x = it & 31;
+  const S s = sv[it];
+  const unsigned nR = B::node_of(rb, head_of(smask[rb], x));
+  int err = 0;
+  if (x == 0 && rel<MODE>(s, scol0[rb])) {
+    if (!sunite(par, (unsigned short)nR, (unsigned short)(B::CNODE + rb))) err = 1;
+  }
+#pragma unroll 1
+  for (int k = 0; k < RowNb<CONN>::n; ++k) {
+    int dy, dz, dxs;
+    row_nb<CONN>(k, dy, dz, dxs);
+    const int rbp = rb + dy + B::BY * dz;
+    unsigned target = 0xFFFFu;
+    if (dxs & 1) {
+      if (x == 0) {
+        if (rel<MODE>(s, scol0[rbp])) target = B::CNODE + rbp;
+      } else if (rel<MODE>(s, sv[rbp * 32 + x - 1])) {
+        target = B::node_of(rbp, head_of(smask[rbp], x - 1));
+      }
+      if (target != 0xFFFFu && !sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
+    }
+    target = 0xFFFFu;
+    if (dxs & 4) {
+      if (x == 31) {
+        if (rel<MODE>(s, scol1[rbp])) target = B::CNODE + B::NRB + rbp;
+      } else if (rel<MODE>(s, sv[rbp * 32 + x + 1])) {
+        target = B::node_of(rbp, head_of(smask[rbp], x + 1));
+      }
+      if (target != 0xFFFFu && !sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
+    }
+  }
+  return err;
+}
+
+template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
+__global__ void __launch_bounds__(kThreads, 4)
+k_tile_runs(LabelArgs p) {
+  using S = typename Stored<T, MODE>::type;
+  constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
+  constexpr int HZ = D3 ? 1 : 0;
+  constexpr int BY = TY + 2, BZ = TZ + HZ;
+  constexpr int NRB = BY * BZ;                 // box rows (tile + halo)
+  constexpr int NR = TY * TZ;                  // tile rows
+  constexpr int HNODE = kTV;                   // halo-row heads: HNODE + rb*32 + lane
+  constexpr int CNODE = kTV + NRB * 32;        // columns: CNODE + rb (x0-1), + NRB + rb (x0+32)
+  constexpr int NODES = CNODE + 2 * NRB;
+  constexpr int NW = kThreads / 32;
+  constexpr int NRN = RowNb<CONN>::n;
+  // neighbour rows (indices into row_nb) whose dx = 0 match makes a voxel's
+  // other backward relations implied; -1 = none
+  constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
+  constexpr int PRI1 = (CONN == 18) ? 0 : -1;
+  constexpr bool HAS_DX = (CONN == 26 || CONN == 18 || CONN == 8);
+  constexpr int QN = 64;                       // per-warp queue capacity
+  static_assert(kTX * NR == kTV, "tile must hold 2048 voxels");
+  static_assert(NR == kRowsPerTile, "64 rows per tile");
+  static_assert(NODES < 16384, "node ids must fit 14 bits");
+  static_assert(!HAS_DX || MODE != MODE_BINARY4, "the binary 4-connected relation has no diagonals");
+
+  __shared__ S sv[NRB * 32];
+  __shared__ S scol[2][NRB];
+  __shared__ uint32_t smask[NRB], fmask[NRB];
+  __shared__ unsigned short par[NODES];
+  __shared__ unsigned short parh[NODES - kTV];   // halo grouping forest (index - kTV)
+  // component ids (phase 3) share their storage with the phase-2 queues
+  __shared__ __align__(16) unsigned short cid[kTV];
+  __shared__ uint32_t rootm[NR];
+  __shared__ unsigned short rbase[NR + 1], cbase[NR + 1];
+  __shared__ uint32_t minblk[BLOCK8 ? kTV : 1];
+  static_assert(NW * QN * (sizeof(uint32_t) + sizeof(unsigned short)) <= sizeof(unsigned short) * kTV,
+                "queues must fit in the component-id storage");
+  uint32_t (*uq)[QN] = reinterpret_cast<uint32_t (*)[QN]>(cid);                       // (a << 16) | b
+  unsigned short (*iq)[QN] = reinterpret_cast<unsigned short (*)[QN]>(cid + 2 * NW * QN);  // rb * 32 + x
+  __shared__ unsigned long long red_epl[NW];
+  __shared__ long long red_first[NW], red_last[NW];
+  __shared__ unsigned int red_prov[NW];
+  __shared__ unsigned int local_err;
+  __shared__ unsigned int edge_fill;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t tile = blockIdx.x;
+  const int tx = (int)(tile % p.ntx);
+  const int64_t rest = tile / p.ntx;
+  const int ty = (int)(rest % p.nty);
+  const int tz = (int)(rest / p.nty);
+  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)ty * TY, z0 = (int64_t)tz * TZ;
+  const T* in = static_cast<const T*>(p.in);
+  const uint32_t lt = (1u << lane) - 1u;
+
+  auto is_tile_row = [&](int rb) -> bool {
+    const int by = rb % BY, bz = rb / BY;
+    return by >= 1 && by <= TY && bz >= HZ;
+  };
+  auto tile_row_of = [&](int rb) -> int { return (rb % BY - 1) + TY * (rb / BY - HZ); };
+  auto box_row_of = [&](int ri) -> int { return (ri / TY + HZ) * BY + (ri % TY) + 1; };
+  // owner code of a halo row / column: which neighbouring tile holds it
+  auto row_owner = [&](int rb) -> int {
+    const int by = rb % BY, bz = rb / BY;
+    return (by == 0 ? 0 : (by == BY - 1 ? 2 : 1)) + 3 * (bz < HZ ? 0 : 1);
+  };
+  auto node_of = [&](int rb, int h) -> unsigned {
+    return is_tile_row(rb) ? (unsigned)(tile_row_of(rb) * 32 + h) : (unsigned)(HNODE + rb * 32 + h);
+  };
+
+  if (tid == 0) {
+    local_err = 0;
+    edge_fill = 0;
+  }
+
+  // ---- phase 0: stage rows and columns, runs, epl on the tile's own rows
+  unsigned long long epl_acc = 0;
+  long long frow = 0x7FFFFFFFFFFFFFFFLL, lrow = -1;
+  for (int rb = warp; rb < NRB; rb += NW) {
+    const int by = rb % BY, bz = rb / BY;
+    const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
+    const bool rowin = (y >= 0) && (y < p.sy) && (z >= 0) && (z < p.sz);
+    const int64_t x = x0 + lane;
+    T v = T(0), vl = T(0), vr = T(0);
+    if (rowin) {
+      const T* rowp = in + (z * p.sy + y) * p.sx;
+      if (x < p.sx) v = rowp[x];
+      if (lane == 0 && x0 > 0) vl = rowp[x0 - 1];
+      if (lane == 0 && x0 + kTX < p.sx) vr = rowp[x0 + kTX];
+    }
+    const S s = to_stored<S, T, MODE>(v);
+    sv[rb * 32 + lane] = s;
+    if (lane == 0) {
+      scol[0][rb] = to_stored<S, T, MODE>(vl);
+      scol[1][rb] = to_stored<S, T, MODE>(vr);
+    }
+    const bool trow = by >= 1 && by <= TY && bz >= HZ;
+    T prev = __shfl_up_sync(FULL, v, 1);
+    if (p.want_epl && trow) {
+      if (lane == 0) prev = vl;
+      const unsigned m = __ballot_sync(FULL, (v != prev) && (v != T(0)));
+      if (m) {
+        epl_acc += __popc(m);
+        const long long rg = (long long)(y + p.sy * z);
+        frow = rg < frow ? rg : frow;
+        lrow = rg > lrow ? rg : lrow;
+      }
+    }
+    if (MODE != MODE_BINARY4) {
+      const S sl = (S)__shfl_up_sync(FULL, s, 1);
+      const bool fg = is_fg(s);
+      bool link = lane > 0 && fg && is_fg(sl);
+      if (MODE == MODE_MULTI) link = link && (s == sl);
+      const uint32_t F = __ballot_sync(FULL, fg);
+      const uint32_t L = __ballot_sync(FULL, link);
+      if (lane == 0) {
+        fmask[rb] = F;
+        smask[rb] = F & ~L;
+      }
+    }
+  }
+  for (int n = tid; n < NODES; n += kThreads) par[n] = (unsigned short)n;
+  for (int n = tid; n < NODES - kTV; n += kThreads) parh[n] = (unsigned short)n;
+  __syncthreads();
+
+  if (MODE == MODE_BINARY4) {
+    // horizontal links of the reference's binary 4-connected labeller: the
+    // first image row links equal values only; later rows drop the link when
+    // both pixels have foreground directly above (they are joined through the
+    // row above).  Halo rows keep single-voxel runs.
+    for (int rb = warp; rb < NRB; rb += NW) {
+      const S s = sv[rb * 32 + lane];
+      const S sl = (S)__shfl_up_sync(FULL, s, 1);
+      const bool fg = is_fg(s);
+      bool link = lane > 0 && fg && is_fg(sl);
+      const int64_t gy = y0 - 1 + rb % BY;
+      if (!is_tile_row(rb)) {
+        link = false;
+      } else if (gy == 0) {
+        link = link && (s == sl);
+      } else {
+        const S a = sv[(rb - 1) * 32 + lane];
+        const S al = (S)__shfl_up_sync(FULL, a, 1);
+        link = link && !(is_fg(a) && is_fg(al));
+      }
+      const uint32_t F = __ballot_sync(FULL, fg);
+      const uint32_t L = __ballot_sync(FULL, link);
+      if (lane == 0) {
+        fmask[rb] = F;
+        smask[rb] = F & ~L;
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- phase 2: unions through per-warp queues
+  int uqn = 0, iqn = 0;  // warp-uniform queue fills
+  unsigned short* P = par;
+  int lim = NODES;
+
+  auto flush_unions = [&](int upto) {
+    // run entries [upto, uqn) in dense rounds of 32
+    __syncwarp();
+    while (uqn > upto) {
+      const int n = uqn - upto < 32 ? uqn - upto : 32;
+      if (lane < n) {
+        const uint32_t e = uq[warp][uqn - n + lane];
+        const int a = (int)(e >> 16), b = (int)(e & 0xFFFFu);
+        if (a >= lim || b >= lim) local_err = 2;
+        else if (!sunite(P, (unsigned short)a, (unsigned short)b)) local_err = 1;
+      }
+      uqn -= n;
+      __syncwarp();
+    }
+  };
+  auto push_unions = [&](uint32_t m, unsigned a, unsigned b) {
+    // lanes in m push (a, b); keeps uqn < 32 between calls
+    if (!m) return;
+    if ((m >> lane) & 1u) uq[warp][uqn + __popc(m & lt)] = (a << 16) | (b & 0xFFFFu);
+    uqn += __popc(m);
+    if (uqn >= 32) flush_unions(uqn - 32 >= 0 ? uqn - 32 : 0);
+  };
+  // one item: a voxel whose primary neighbour does not match tests its dx = +-1
+  // neighbours and the halo columns
+  auto flush_items = [&](int upto) {
+    __syncwarp();
+    while (iqn > upto) {
+      const int n = iqn - upto < 32 ? iqn - upto : 32;
+      if (lane < n) {
+        if (tile_item<S, CONN, TY, TZ, MODE>(iq[warp][iqn - n + lane], sv, scol[0], scol[1], smask, par))
+          local_err = 1;
+      }
+      iqn -= n;
+      __syncwarp();
+    }
+  };
+
+  // tile rows
+  for (int ri = warp; ri < NR; ri += NW) {
+    const int rb = box_row_of(ri);
+    const S s = sv[rb * 32 + lane];
+    const uint32_t F = fmask[rb], Sr = smask[rb];
+    const bool fg = (F >> lane) & 1u;
+    const unsigned nR = (unsigned)(ri * 32 + head_of(Sr, lane));
+    uint32_t M0[NRN], Sp[NRN];
+#pragma unroll
+    for (int k = 0; k < NRN; ++k) {
+      int dy, dz, dxs;
+      row_nb<CONN>(k, dy, dz, dxs);
+      const int rbp = rb + dy + BY * dz;
+      const S w = sv[rbp * 32 + lane];
+      Sp[k] = smask[rbp];
+      M0[k] = __ballot_sync(FULL, fg && rel<MODE>(s, w));
+    }
+    uint32_t SC = 0;
+    if (PRI0 >= 0) SC = M0[PRI0 < 0 ? 0 : PRI0];
+    if (PRI1 >= 0) SC &= M0[PRI1 < 0 ? 0 : PRI1];
+    const uint32_t NEED = (PRI0 >= 0) ? (F & ~SC) : F;
+#pragma unroll
+    for (int k = 0; k < NRN; ++k) {
+      int dy, dz, dxs;
+      row_nb<CONN>(k, dy, dz, dxs);
+      const int rbp = rb + dy + BY * dz;
+      const bool primary = (k == PRI0) || (k == PRI1);
+      uint32_t U = M0[k] & (Sr | Sp[k] | ~(M0[k] << 1));
+      if (!primary) U &= NEED;
+      push_unions(U, nR, node_of(rbp, head_of(Sp[k], lane)));
+    }
+    if (HAS_DX) {
+      // voxels not covered by their primary neighbour become items
+      if (NEED) {
+        if ((NEED >> lane) & 1u) iq[warp][iqn + __popc(NEED & lt)] = (unsigned short)(rb * 32 + lane);
+        iqn += __popc(NEED);
+        if (iqn >= 32) flush_items(iqn - 32 >= 0 ? iqn - 32 : 0);
+      }
+    } else if (F & 1u) {
+      // same-row neighbour across the x seam
+      const S s0 = (S)__shfl_sync(FULL, s, 0);
+      const S c0 = scol[0][rb];
+      bool r0;
+      if (MODE == MODE_MULTI) r0 = (s0 == c0);
+      else if (MODE == MODE_BINARY4) {
+        const int64_t gy = y0 - 1 + rb % BY;
+        r0 = is_fg(c0) && (gy == 0 ? (s0 == c0)
+                                   : !(is_fg(sv[(rb - 1) * 32]) && is_fg(scol[0][rb - 1])));
+      } else r0 = is_fg(c0);
+      if (r0) push_unions(1u, (unsigned)(ri * 32), (unsigned)(CNODE + rb));
+    }
+  }
+  flush_items(0);
+  flush_unions(0);
+
+  // halo rows: group with backward halo rows of the same owner (dx = 0 only;
+  // an incomplete grouping only costs extra edges)
+  P = parh;
+  lim = NODES - kTV;
+  if (MODE != MODE_BINARY4) {
+    for (int rb = warp; rb < NRB; rb += NW) {
+      if (is_tile_row(rb)) continue;
+      const S s = sv[rb * 32 + lane];
+      const uint32_t F = fmask[rb], Sr = smask[rb];
+      const bool fg = (F >> lane) & 1u;
+      const int own = row_owner(rb);
+      const unsigned nR = (unsigned)(rb * 32 + head_of(Sr, lane));
+#pragma unroll
+      for (int k = 0; k < NRN; ++k) {
+        int dy, dz, dxs;
+        row_nb<CONN>(k, dy, dz, dxs);
+        const int by = rb % BY + dy, bz = rb / BY + dz;
+        if (by < 0 || by >= BY || bz < 0 || bz >= BZ) continue;
+        const int rbp = rb + dy + BY * dz;
+        if (is_tile_row(rbp) || row_owner(rbp) != own) continue;
+        const S w = sv[rbp * 32 + lane];
+        const uint32_t Spk = smask[rbp];
+        const uint32_t M = __ballot_sync(FULL, fg && rel<MODE>(s, w));
+        push_unions(M & (Sr | Spk | ~(M << 1)), nR, (unsigned)(rbp * 32 + head_of(Spk, lane)));
+      }
+    }
+    flush_unions(0);
+    // halo columns: group with backward voxels of the same column and owner
+    for (int c = tid; c < 2 * NRB; c += kThreads) {
+      const int side = c / NRB, rb = c % NRB;
+      const S s = scol[side][rb];
+      if (!is_fg(s)) continue;
+      const int own = row_owner(rb);
+#pragma unroll
+      for (int k = 0; k < NRN; ++k) {
+        int dy, dz, dxs;
+        row_nb<CONN>(k, dy, dz, dxs);
+        if (!(dxs & 2)) continue;
+        const int by = rb % BY + dy, bz = rb / BY + dz;
+        if (by < 0 || by >= BY || bz < 0 || bz >= BZ) continue;
+        const int rbp = rb + dy + BY * dz;
+        if (row_owner(rbp) != own) continue;
+        if (rel<MODE>(s, scol[side][rbp]))
+          if (!sunite(parh, (unsigned short)(CNODE - kTV + c), (unsigned short)(CNODE - kTV + side * NRB + rbp)))
+            local_err = 1;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 3a: component roots per tile row, run counts per row
+  for (int ri = warp; ri < NR; ri += NW) {
+    const int rb = box_row_of(ri);
+    const uint32_t Sr = smask[rb];
+    bool root = false;
+    if ((Sr >> lane) & 1u) {
+      const unsigned short n = (unsigned short)(ri * 32 + lane);
+      const unsigned short r = sfind_ro(par, n);
+      par[n] = r;
+      root = (r == n);
+    }
+    const uint32_t rm = __ballot_sync(FULL, root);
+    if (lane == 0) {
+      rootm[ri] = rm;
+      rbase[ri + 1] = (unsigned short)__popc(Sr);
+      cbase[ri + 1] = (unsigned short)__popc(rm);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // exclusive prefix over the 64 rows (two per lane)
+    const uint32_t a0 = rbase[2 * lane + 1], a1 = rbase[2 * lane + 2];
+    const uint32_t c0 = cbase[2 * lane + 1], c1 = cbase[2 * lane + 2];
+    uint32_t sa = a0 + a1, sc = c0 + c1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t ya = __shfl_up_sync(FULL, sa, o), yc = __shfl_up_sync(FULL, sc, o);
+      if (lane >= o) { sa += ya; sc += yc; }
+    }
+    rbase[2 * lane + 1] = (unsigned short)(sa - a1);
+    rbase[2 * lane + 2] = (unsigned short)sa;
+    cbase[2 * lane + 1] = (unsigned short)(sc - c1);
+    cbase[2 * lane + 2] = (unsigned short)sc;
+    if (lane == 0) { rbase[0] = 0; cbase[0] = 0; }
+  }
+  __syncthreads();
+  for (int ri = warp; ri < NR; ri += NW) {
+    const uint32_t rm = rootm[ri];
+    if ((rm >> lane) & 1u) cid[ri * 32 + lane] = (unsigned short)(cbase[ri] + __popc(rm & lt));
+  }
+  const uint32_t C = cbase[NR];
+  if (BLOCK8)
+    for (uint32_t c = tid; c < C; c += kThreads) minblk[c] = 0xFFFFFFFFu;
+  __syncthreads();
+
+  // ---- phase 3b: run records, keys, bitmap
+  const uint32_t node0 = (uint32_t)(tile * kTV);
+  for (int ri = warp; ri < NR; ri += NW) {
+    const int rb = box_row_of(ri);
+    const uint32_t Sr = smask[rb], F = fmask[rb];
+    const int ly = ri % TY, lz = ri / TY;
+    const int64_t y = y0 + ly, z = z0 + lz;
+    if (lane == 0) {
+      p.rmask[tile * kRowsPerTile + ri] = make_uint2(F, Sr);
+      p.rrow[tile * kRowsPerTile + ri] = rbase[ri];
+    }
+    if ((Sr >> lane) & 1u) {
+      const unsigned short r = par[ri * 32 + lane];
+      const unsigned short c = cid[r];
+      p.rcomp[tile * kTV + rbase[ri] + __popc(Sr & lt)] = c;
+      if (BLOCK8) atomicMin(&minblk[c], (uint32_t)((y >> 1) * p.key_row + ((x0 + lane) >> 1)));
+    }
+    if (!BLOCK8) {
+      const uint32_t rm = rootm[ri];
+      if ((rm >> lane) & 1u) {
+        const uint32_t key = (uint32_t)((z * p.sy + y) * p.key_row + x0 + lane);
+        const uint32_t c = cid[ri * 32 + lane];
+        p.E[node0 + c] = ((unsigned long long)key << 32) | (node0 + c);
+      }
+      if (lane == 0 && y < p.sy && z < p.sz) p.bitmap[(z * p.sy + y) * p.wpr + tx] = rm;
+    }
+  }
+  if (BLOCK8) {
+    __syncthreads();
+    for (uint32_t c = tid; c < C; c += kThreads) {
+      const uint32_t key = minblk[c];
+      atomicOr(p.bitmap + (key >> 5), 1u << (key & 31));
+      p.E[node0 + c] = ((unsigned long long)key << 32) | (node0 + c);
+    }
+  }
+
+  // ---- phase 3c: one edge per (tile component, halo group) into the tile's
+  // own edge slots
+  auto halo_edge = [&](int h, uint2& e) -> bool {
+    int rb, lx;
+    int64_t gx;
+    bool fg;
+    if (h < NRB * 32) {
+      rb = h >> 5;
+      lx = h & 31;
+      if (is_tile_row(rb)) return false;
+      fg = ((smask[rb] >> lx) & 1u) != 0;  // run heads stand for their runs
+      gx = x0 + lx;
+    } else {
+      const int c = h - NRB * 32;
+      rb = c % NRB;
+      fg = is_fg(scol[c / NRB][rb]);
+      gx = (c < NRB) ? x0 - 1 : x0 + kTX;
+      lx = (int)(gx & 31);
+    }
+    if (!fg) return false;
+    const unsigned short r = sfind_ro(par, (unsigned short)(kTV + h));
+    if (r >= kTV) return false;
+    const unsigned short g = sfind_ro(parh, (unsigned short)h);
+    if (g != h && sfind_ro(par, (unsigned short)(kTV + g)) == r) return false;
+    const int by = rb % BY, bz = rb / BY;
+    const int64_t gy = y0 - 1 + by, gz = z0 - HZ + bz;
+    const int64_t otile = (gx >> 5) + (int64_t)p.ntx * ((gy / TY) + (int64_t)p.nty * (gz / TZ));
+    const uint32_t local = (uint32_t)(lx + kTX * ((gy % TY) + TY * (gz % TZ)));
+    e = make_uint2(node0 + cid[r], (uint32_t)(otile * kTV + local));
+    return true;
+  };
+  uint2* edges = p.edges + tile * p.edge_slots;
+  constexpr int NCC = (2 * NRB + 31) / 32;  // 32-voxel chunks of the two halo columns
+  for (int it = warp; it < NRB + NCC; it += NW) {
+    int h;
+    if (it < NRB) {
+      if (is_tile_row(it)) continue;
+      h = it * 32 + lane;
+    } else {
+      const int c = (it - NRB) * 32 + lane;
+      h = c < 2 * NRB ? NRB * 32 + c : -1;
+    }
+    uint2 e;
+    const bool has = h >= 0 && halo_edge(h, e);
+    const unsigned m = __ballot_sync(FULL, has);
+    if (!m) continue;
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&edge_fill, (unsigned)__popc(m));
+    base = __shfl_sync(FULL, base, 0);
+    if (has) {
+      const unsigned slot = base + __popc(m & lt);
+      if (slot < p.edge_slots) edges[slot] = e;
+    }
+  }
+
+  // ---- provisional labels the reference's binary labeller would open
+  unsigned int prov = 0;
+  if (p.want_prov) {
+    if (BLOCK8) {
+      // 2x2 blocks Y Z / X W; C D E F in the row above, B A to the left
+      for (int q = tid; q < kTV / 4; q += kThreads) {
+        const int b = q & 15, ri = 2 * (q >> 4);
+        const int rb = box_row_of(ri);
+        const uint32_t Fa = fmask[rb - 1], F0 = fmask[rb], F1 = fmask[rb + 1];
+        const uint32_t ca = is_fg(scol[0][rb - 1]) ? 1u : 0u, c0 = is_fg(scol[0][rb]) ? 1u : 0u;
+        const uint32_t c1 = is_fg(scol[0][rb + 1]) ? 1u : 0u, ra = is_fg(scol[1][rb - 1]) ? 1u : 0u;
+        const int x = 2 * b;
+        const bool Y = (F0 >> x) & 1u, Z = (F0 >> (x + 1)) & 1u;
+        const bool X = (F1 >> x) & 1u, W = (F1 >> (x + 1)) & 1u;
+        if (!(Y || Z || X || W)) continue;
+        const bool Cc = x == 0 ? ca : (Fa >> (x - 1)) & 1u;
+        const bool D = (Fa >> x) & 1u, Ee = (Fa >> (x + 1)) & 1u;
+        const bool Fq = x + 2 == 32 ? ra : (Fa >> (x + 2)) & 1u;
+        const bool B = x == 0 ? c0 : (F0 >> (x - 1)) & 1u;
+        const bool A = x == 0 ? c1 : (F1 >> (x - 1)) & 1u;
+        const bool linked = (Y && (Cc || D || Ee || B || A)) || (Z && (D || Ee || Fq)) || (X && (B || A));
+        prov += linked ? 0u : 1u;
+      }
+    } else {
+      for (int ri = warp; ri < NR; ri += NW) {
+        const int rb = box_row_of(ri);
+        const uint32_t F = fmask[rb];
+        const S s = sv[rb * 32 + lane];
+        uint32_t Lk;
+        const int64_t gy = y0 + ri % TY, gz = z0 + ri / TY;
+        if (MODE == MODE_BINARY4 && gy == 0 && gz == 0) {
+          S sl = (S)__shfl_up_sync(FULL, s, 1);
+          if (lane == 0) sl = scol[0][rb];
+          Lk = __ballot_sync(FULL, is_fg(s) && s == sl);
+        } else {
+          Lk = (F << 1) | (is_fg(scol[0][rb]) ? 1u : 0u);
+        }
+#pragma unroll
+        for (int k = 0; k < NRN; ++k) {
+          int dy, dz, dxs;
+          row_nb<CONN>(k, dy, dz, dxs);
+          const int rbp = rb + dy + BY * dz;
+          const uint32_t Fp = fmask[rbp];
+          if (dxs & 2) Lk |= Fp;
+          if (dxs & 1) Lk |= (Fp << 1) | (is_fg(scol[0][rbp]) ? 1u : 0u);
+          if (dxs & 4) Lk |= (Fp >> 1) | (is_fg(scol[1][rbp]) ? 0x80000000u : 0u);
+        }
+        if (lane == 0) prov += __popc(F & ~Lk);
+      }
+    }
+  }
+
+  // ---- reductions
+  if (lane == 0) {
+    red_epl[warp] = epl_acc;
+    red_first[warp] = frow;
+    red_last[warp] = lrow;
+  }
+  unsigned int pw = prov;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pw += __shfl_down_sync(FULL, pw, o);
+  if (lane == 0) red_prov[warp] = pw;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long e = 0, pv = 0;
+    long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+    for (int w = 0; w < NW; ++w) {
+      e += red_epl[w];
+      pv += red_prov[w];
+      f = red_first[w] < f ? red_first[w] : f;
+      l = red_last[w] > l ? red_last[w] : l;
+    }
+    const uint32_t nedges = edge_fill;
+    TileInfo ti;
+    ti.C = C;
+    ti.nedges = nedges < p.edge_slots ? nedges : p.edge_slots;
+    ti.epl = (uint32_t)e;
+    ti.prov = (uint32_t)pv;
+    ti.first_row = f;
+    ti.last_row = l;
+    p.tinfo[tile] = ti;
+    if (nedges > p.edge_slots) atomicOr(&p.ctr->err, ERR_EDGE_OVERFLOW);
+    if (local_err) atomicOr(&p.ctr->err, local_err == 2 ? ERR_INDEX : ERR_LOCAL_BUDGET);
+  }
+}
+
+}  // namespace cc3dgpu

@@ -94,6 +94,39 @@ int cc3d_gpu_connected_components3d(
     int mem_flags, void* stream);
 
 /*
+ * The same labelling in two steps, for callers that choose the output dtype
+ * from the provisional-label estimate, as the reference's Cython layer does
+ * (cc3d/fastcc3d.pyx:386-434): the estimate is computed in the same pass over
+ * the input as the labelling, so the volume is read once.
+ *
+ * cc3d_gpu_label_prepare runs every stage up to the numbering and returns the
+ * estimate (epl, first/last foreground row; for binary images the values the
+ * Cython layer substitutes: voxels, 0, sy), the number of components N and a
+ * token.  cc3d_gpu_label_finish(token, ...) then writes the labels in the
+ * chosen dtype; it must be called on the same thread before any other call of
+ * this library on that thread.  max_labels and the error cases are as for
+ * cc3d_gpu_connected_components3d.
+ */
+typedef struct {
+  uint64_t token;
+  uint64_t epl;
+  int64_t first_row;
+  int64_t last_row;
+  uint64_t N;
+  uint64_t provisional;  /* provisional labels the reference's binary labeller opens */
+  uint64_t edges;        /* tile-boundary edges merged (a measure of boundary work) */
+} cc3d_gpu_prepared;
+
+int cc3d_gpu_label_prepare(
+    const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+    int64_t connectivity, int periodic_boundary, int binary_image,
+    int mem_flags, void* stream, cc3d_gpu_prepared* info);
+
+int cc3d_gpu_label_finish(
+    uint64_t token, int64_t max_labels, void* out, int out_dtype, uint64_t* N,
+    int mem_flags, void* stream);
+
+/*
  * The single-foreground-row case of the Cython layer: the foreground row
  * `row` (0-based over sy*sz rows) is labelled run by run, keeping the previous
  * run's value in a C int64 as the reference does.  Writes only that row of

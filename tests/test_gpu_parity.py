@@ -158,3 +158,24 @@ def test_voronoi_128_config(cc3d):
     for conn in (26, 18, 6):
         _compare(cc3d.connected_components, vol, dict(connectivity=conn))
         _compare(_on_device(cc3d.connected_components), vol, dict(connectivity=conn))
+
+
+def test_repeatable_under_concurrency(cc3d):
+    """The same volume labelled many times gives identical labels (a check on
+    the lock-free union-finds), and equals the oracle."""
+    import torch
+    from cc3d_gb300 import synth
+    vol = synth.voronoi_volume((160, 192, 224), n_seeds=600, label_max=1 << 20, seed=11)
+    exp, eN = oracle.connected_components(vol, connectivity=26, return_N=True)
+    dev = torch.from_numpy(vol).cuda()
+    for _ in range(12):
+        out, N = cc3d.connected_components(dev, connectivity=26, return_N=True)
+        assert N == eN
+        assert np.array_equal(out.cpu().numpy(), exp)
+    b = synth.bernoulli_volume((128, 160, 192), 0.3116, seed=5)
+    expb = oracle.connected_components(b, connectivity=6, binary_image=True, return_N=True)
+    devb = torch.from_numpy(b).cuda()
+    for _ in range(6):
+        out, N = cc3d.connected_components(devb, connectivity=6, binary_image=True, return_N=True)
+        assert N == expb[1]
+        assert np.array_equal(out.cpu().numpy(), expb[0])
