@@ -153,11 +153,12 @@ cudaStream_t pick_stream(Workspace& w, void* stream, int mem_flags) {
 int check_device_errors(unsigned err) {
   if (!err) return CC3D_OK;
   return fail(CC3D_ERR_DEVICE,
-              "device kernel gave up (error bits 0x%x: %s%s%s%s%s)", err,
+              "device kernel gave up (error bits 0x%x: %s%s%s%s%s%s)", err,
               (err & ERR_UNITE_BUDGET) ? "union budget " : "",
               (err & ERR_FIND_BUDGET) ? "find budget " : "",
               (err & ERR_EDGE_OVERFLOW) ? "edge buffer overflow " : "",
               (err & ERR_LOCAL_BUDGET) ? "tile union budget " : "",
+              (err & ERR_WAIT) ? "input copy never completed " : "",
               (err & ERR_INDEX) ? "index range check" : "");
 }
 

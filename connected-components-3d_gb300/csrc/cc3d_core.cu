@@ -4,6 +4,19 @@
 
 namespace cc3dgpu {
 
+void* tensor_map_encoder() {
+  static void* fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return f;
+  }();
+  return fn;
+}
+
 // ------------------------------------------------------- K2: edge merges
 // Every edge joins a tile component (x = its node) with the component that
 // owns a halo voxel in the neighbouring tile (y = tile * 2048 + voxel index).

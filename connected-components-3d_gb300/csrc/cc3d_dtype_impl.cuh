@@ -3,6 +3,9 @@
 // launchers declared in cc3d_internal.h through CC3D_DEFINE_DTYPE_LAUNCHERS.
 #pragma once
 
+#include <cstring>
+#include <type_traits>
+
 #include "cc3d_internal.h"
 
 namespace cc3dgpu {
@@ -161,9 +164,50 @@ __global__ void __launch_bounds__(256) k_minmax(const T* in, int64_t n, int is_s
 }
 
 // ------------------------------------------------------------- launchers
-template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
+template <typename T>
+constexpr CUtensorMapDataType tma_type() {
+  return sizeof(T) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+         : sizeof(T) == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+         : sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                          : CU_TENSOR_MAP_DATA_TYPE_UINT64;
+}
+
+// The scan streams its box rows through TMA when the volume allows it: a
+// 16-byte aligned base and rows whose byte length is a multiple of 16 (the
+// copy engine's stride rule).  Otherwise the warps load the rows themselves.
+template <typename T, int CONN, int TY, int TZ, int MODE>
 cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  k_tile_runs<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  using G = ScanGeom<T, CONN, TY, TZ>;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  int use_tma = 0;
+  const bool aligned = ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
+                       a.sx < (1ll << 31) && a.sy < (1ll << 31) && a.sz < (1ll << 31);
+  if (aligned && ntiles > 0) {
+    using Encode = decltype(&cuTensorMapEncodeTiled);
+    if (Encode enc = reinterpret_cast<Encode>(tensor_map_encoder())) {
+      const cuuint64_t dims[3] = {(cuuint64_t)a.sx, (cuuint64_t)a.sy, (cuuint64_t)a.sz};
+      const cuuint64_t strides[2] = {(cuuint64_t)(a.sx * sizeof(T)), (cuuint64_t)(a.sx * a.sy * sizeof(T))};
+      const cuuint32_t box[3] = {(cuuint32_t)G::W, (cuuint32_t)G::CH, 1u};
+      const cuuint32_t estr[3] = {1u, 1u, 1u};
+      use_tma = enc(&map, tma_type<T>(), 3, const_cast<void*>(a.in), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+  }
+  const size_t smem = scan_smem_bytes<T, CONN, TY, TZ>();
+  cudaError_t e = cudaFuncSetAttribute(k_tile_scan<T, CONN, TY, TZ, MODE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = (ntiles + kScanWarps - 1) / kScanWarps;
+  k_tile_scan<T, CONN, TY, TZ, MODE><<<(unsigned)blocks, kScanWarps * 32, smem, s>>>(a, map, use_tma);
+  return cudaGetLastError();
+}
+
+// binary 8-connected images are numbered by 2x2 blocks: the block-parallel pass
+template <typename T>
+cudaError_t launch_k1_block8(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  k_tile_runs<T, 8, 64, 1, MODE_BINARY, true><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -173,26 +217,26 @@ cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool blo
   switch (conn) {
     case 26:
       if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 26, 8, 8, MODE_MULTI, false>(a, ntiles, s)
-                                : launch_k1<T, 26, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+      return mode == MODE_MULTI ? launch_k1<T, 26, 8, 8, MODE_MULTI>(a, ntiles, s)
+                                : launch_k1<T, 26, 8, 8, MODE_BINARY>(a, ntiles, s);
     case 18:
       if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 18, 8, 8, MODE_MULTI, false>(a, ntiles, s)
-                                : launch_k1<T, 18, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+      return mode == MODE_MULTI ? launch_k1<T, 18, 8, 8, MODE_MULTI>(a, ntiles, s)
+                                : launch_k1<T, 18, 8, 8, MODE_BINARY>(a, ntiles, s);
     case 6:
       if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 6, 8, 8, MODE_MULTI, false>(a, ntiles, s)
-                                : launch_k1<T, 6, 8, 8, MODE_BINARY, false>(a, ntiles, s);
+      return mode == MODE_MULTI ? launch_k1<T, 6, 8, 8, MODE_MULTI>(a, ntiles, s)
+                                : launch_k1<T, 6, 8, 8, MODE_BINARY>(a, ntiles, s);
     case 8:
       if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
-      if (mode == MODE_MULTI) return launch_k1<T, 8, 64, 1, MODE_MULTI, false>(a, ntiles, s);
-      if (block8) return launch_k1<T, 8, 64, 1, MODE_BINARY, true>(a, ntiles, s);
-      return launch_k1<T, 8, 64, 1, MODE_BINARY, false>(a, ntiles, s);
+      if (mode == MODE_MULTI) return launch_k1<T, 8, 64, 1, MODE_MULTI>(a, ntiles, s);
+      if (block8) return launch_k1_block8<T>(a, ntiles, s);
+      return launch_k1<T, 8, 64, 1, MODE_BINARY>(a, ntiles, s);
     case 4:
       if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
-      if (mode == MODE_MULTI) return launch_k1<T, 4, 64, 1, MODE_MULTI, false>(a, ntiles, s);
-      if (mode == MODE_BINARY4) return launch_k1<T, 4, 64, 1, MODE_BINARY4, false>(a, ntiles, s);
-      return launch_k1<T, 4, 64, 1, MODE_BINARY, false>(a, ntiles, s);
+      if (mode == MODE_MULTI) return launch_k1<T, 4, 64, 1, MODE_MULTI>(a, ntiles, s);
+      if (mode == MODE_BINARY4) return launch_k1<T, 4, 64, 1, MODE_BINARY4>(a, ntiles, s);
+      return launch_k1<T, 4, 64, 1, MODE_BINARY>(a, ntiles, s);
   }
   return cudaErrorInvalidValue;
 }

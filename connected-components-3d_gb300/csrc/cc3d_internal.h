@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "cc3d_label.cuh"
+#include "cc3d_scan.cuh"
 #include "cc3d_tile.cuh"
 
 namespace cc3dgpu {
@@ -30,6 +31,10 @@ CC3D_DECLARE_DTYPE_LAUNCHERS(u32)
 CC3D_DECLARE_DTYPE_LAUNCHERS(u64)
 CC3D_DECLARE_DTYPE_LAUNCHERS(f32)
 CC3D_DECLARE_DTYPE_LAUNCHERS(f64)
+
+// cuTensorMapEncodeTiled from the driver (null if the driver lacks it);
+// fetched once through the runtime, so the library needs no -lcuda
+void* tensor_map_encoder();
 
 // dtype-independent stages (cc3d_core.cu)
 cudaError_t launch_merge_edges(const LabelArgs& a, cudaStream_t s);
