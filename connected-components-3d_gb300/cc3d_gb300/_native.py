@@ -37,6 +37,7 @@ EXPORTED = (
     "cc3d_gpu_profile_enable",
     "cc3d_gpu_profile_read",
     "cc3d_gpu_release_workspace",
+    "cc3d_gpu_connected_components3d_noalloc",
 )
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
 
@@ -83,6 +84,9 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_label_minmax.argtypes = [vp, ci, ci, i64, u64p, i64p, ci, vp]
         lib.cc3d_gpu_statistics.argtypes = [vp, ci, i64, i64, i64, ci, ci, ctypes.c_uint64, vp, vp, ci, vp, ci, vp]
         lib.cc3d_gpu_release_workspace.restype = None
+        lib.cc3d_gpu_connected_components3d_noalloc.argtypes = [
+            vp, ci, i64, i64, i64, i64, i64, vp, ci, u64p, ci, ci, vp]
+        lib.cc3d_gpu_connected_components3d_noalloc.restype = ctypes.c_int
         lib.cc3d_gpu_profile_enable.argtypes = [ci]
         lib.cc3d_gpu_profile_enable.restype = None
         lib.cc3d_gpu_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), u64p, ci]

@@ -214,6 +214,10 @@ struct StageTimer {
 
 }  // namespace
 
+// error reporting shared with the other host translation units
+int cc3dgpu::api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+int cc3dgpu::api_device_errors(unsigned err) { return check_device_errors(err); }
+
 extern "C" {
 
 void cc3d_gpu_profile_enable(int enable) { g_prof.on = enable != 0; }

@@ -36,6 +36,11 @@ CC3D_DECLARE_DTYPE_LAUNCHERS(f64)
 // fetched once through the runtime, so the library needs no -lcuda
 void* tensor_map_encoder();
 
+// set the calling thread's error message (returns code); map a device error
+// word to a return code (cc3d_capi.cu)
+int api_fail(int code, const char* msg);
+int api_device_errors(unsigned err);
+
 // dtype-independent stages (cc3d_core.cu)
 cudaError_t launch_merge_edges(const LabelArgs& a, cudaStream_t s);
 cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* block_sums,

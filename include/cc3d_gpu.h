@@ -185,6 +185,39 @@ int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
 /* Release this thread's cached device workspace. */
 void cc3d_gpu_release_workspace(void);
 
+/*
+ * Labelling that allocates nothing.  No counterpart in the reference: the
+ * reference labels on the CPU into a buffer its caller allocated and needs no
+ * device scratch.
+ *
+ * Same arguments, results and errors as cc3d_gpu_connected_components3d with
+ * delta = 0, for DEVICE input and output buffers only.  Instead of the
+ * per-thread workspace the other entry points grow with cudaMalloc, all
+ * scratch comes from one fixed array of CC3D_NOALLOC_SCRATCH_BYTES that is part
+ * of the library's device image, held by every GPU that loads the library
+ * until the process exits.  For callers that cannot allocate device memory
+ * while they label: memory owned by another allocator's pool, a fixed memory
+ * budget, or loops where cudaMalloc/cudaFree latency and cudaFree's
+ * device-wide wait are not acceptable.
+ *   - Limit: the scratch of a volume is about 37 KB per 32x8x8 tile (3D) or
+ *     31 KB per 32x64 tile (2D), so 128x128x128 (1024 tiles) fits; a larger
+ *     volume returns CC3D_ERR_INVALID with the bytes it would need.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call uses the same array, which keeps the last call's contents;
+ *     calls whose GPU work overlaps (other threads, unordered streams) race
+ *     and corrupt each other's results.
+ *   - Allocates no device or pinned memory; N and the device error word come
+ *     back through host stack memory, and the call returns when labels are
+ *     written.
+ */
+#define CC3D_NOALLOC_SCRATCH_BYTES 41943040u /* 40 MiB */
+int cc3d_gpu_connected_components3d_noalloc(
+    const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+    int64_t max_labels, int64_t connectivity,
+    void* out, int out_dtype, uint64_t* N,
+    int periodic_boundary, int binary_image, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
