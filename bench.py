@@ -326,6 +326,66 @@ def run_gpu(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ all workloads
+def _workloads():
+    """The benchmarked workloads: (name, volume factory, labelling kwargs)."""
+    from cc3d_gb300 import synth
+    vor512 = lambda: synth.voronoi_volume((512, 512, 512), 4096, 1 << 20, seed=1, dtype=np.uint32)  # noqa: E731
+    out = [("voronoi512_u32_c%d" % c, vor512, dict(connectivity=c)) for c in (26, 18, 6)]
+    out.append(("voronoi768_u64_c26", lambda: synth.voronoi_volume((768, 768, 768), 4096, 1 << 48, seed=2,
+                                                                   dtype=np.uint64),
+                dict(connectivity=26, out_dtype=np.uint64)))
+    for p in (0.2, 0.3116, 0.5):
+        f = (lambda p=p: synth.bernoulli_volume((512, 512, 512), p, seed=int(p * 1e4)))
+        for c in (6, 18, 26):
+            out.append((f"bernoulli{p}_512_u8_c{c}_binary", f, dict(connectivity=c, binary_image=True)))
+        out.append((f"bernoulli{p}_512_u8_c6_binary_periodic", f,
+                    dict(connectivity=6, binary_image=True, periodic_boundary=True)))
+    img = lambda: synth.bernoulli_volume((8192, 8192), 0.5, seed=8192)  # noqa: E731
+    for c in (8, 4):
+        for b in (True, False):
+            out.append((f"bernoulli0.5_8192x8192_u8_c{c}_{'binary' if b else 'multilabel'}", img,
+                        dict(connectivity=c, binary_image=b)))
+    return out
+
+
+def run_all_configs(args):
+    """One JSON line per workload: device-resident GVoxels/s of each tile-pass
+    variant and of the autotuned choice (CUDA events, input larger than L2)."""
+    import torch
+    import cc3d_gb300 as cc3d
+    cc3d.build()
+    cache = {}
+    for name, make, kw in _workloads():
+        key = make
+        if key not in cache:
+            cache.clear()
+            cache[key] = torch.from_numpy(make()).cuda()
+        dev = cache[key]
+        res = {}
+        for variant in ("runs", "scan", "auto"):
+            if variant == "auto":
+                cc3d.set_tile_pass("auto")
+                tuned = cc3d.autotune(dev, connectivity=kw["connectivity"],
+                                      binary_image=kw.get("binary_image", False))
+            else:
+                cc3d.set_tile_pass(variant)
+            for _ in range(args.warmup):
+                cc3d.connected_components(dev, **kw)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                _, n = cc3d.connected_components(dev, return_N=True, **kw)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            res[variant] = {"ms": ms, "GVoxels/s": dev.numel() / ms / 1e6}
+        cc3d.set_tile_pass("auto")
+        print(json.dumps({"workload": name, "N": n, "voxels": dev.numel(), "tuned": tuned["best"],
+                          "variants": res}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,6 +395,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--size", type=int, default=512, help="cube edge (profiling captures only)")
+    ap.add_argument("--all-configs", action="store_true",
+                    help="one line per benchmarked workload and tile-pass variant instead of the headline")
     args = ap.parse_args()
     global SHAPE, N_SEEDS
     if args.size != 512:
@@ -342,6 +404,9 @@ def main():
         N_SEEDS = max(1, 4096 * args.size ** 3 // 512 ** 3)
     if args.warmup < 3:
         args.warmup = 3
+    if args.all_configs:
+        run_all_configs(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

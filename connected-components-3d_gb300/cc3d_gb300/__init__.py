@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     statistics,
 )
 from . import _native  # noqa: F401
+from .tuning import autotune, autotune_reset, set_tile_pass, tile_pass_choice  # noqa: F401
 
 __all__ = [
     "build",
@@ -19,4 +20,8 @@ __all__ = [
     "estimate_provisional_labels",
     "statistics",
     "DimensionError",
+    "autotune",
+    "autotune_reset",
+    "set_tile_pass",
+    "tile_pass_choice",
 ]

@@ -38,7 +38,12 @@ EXPORTED = (
     "cc3d_gpu_profile_read",
     "cc3d_gpu_release_workspace",
     "cc3d_gpu_connected_components3d_noalloc",
+    "cc3d_gpu_set_tile_pass",
+    "cc3d_gpu_tile_pass_choice",
+    "cc3d_gpu_autotune",
+    "cc3d_gpu_autotune_reset",
 )
+TILE_PASSES = {"auto": 0, "runs": 1, "scan": 2}
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
 
 class Prepared(ctypes.Structure):
@@ -87,6 +92,15 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_connected_components3d_noalloc.argtypes = [
             vp, ci, i64, i64, i64, i64, i64, vp, ci, u64p, ci, ci, vp]
         lib.cc3d_gpu_connected_components3d_noalloc.restype = ctypes.c_int
+        lib.cc3d_gpu_set_tile_pass.argtypes = [ci]
+        lib.cc3d_gpu_set_tile_pass.restype = ci
+        lib.cc3d_gpu_tile_pass_choice.argtypes = [ci, i64, i64, i64, i64, ci]
+        lib.cc3d_gpu_tile_pass_choice.restype = ci
+        lib.cc3d_gpu_autotune.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, ci,
+                                          ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_double)]
+        lib.cc3d_gpu_autotune.restype = ci
+        lib.cc3d_gpu_autotune_reset.argtypes = []
+        lib.cc3d_gpu_autotune_reset.restype = None
         lib.cc3d_gpu_profile_enable.argtypes = [ci]
         lib.cc3d_gpu_profile_enable.restype = None
         lib.cc3d_gpu_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), u64p, ci]

@@ -1,0 +1,84 @@
+"""Tile-pass variants and their autotuner (include/cc3d_gpu.h: cc3d_gpu_set_tile_pass,
+cc3d_gpu_tile_pass_choice, cc3d_gpu_autotune, cc3d_gpu_autotune_reset).
+
+Every variant labels identically; the autotuner only picks the faster one for a
+class of volumes (dtype, effective connectivity, binary or not, voxel count
+within a factor of 8) and the labelling entry points use that choice from then
+on.  The reference has no counterpart: it runs one CPU algorithm per
+connectivity.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Any, Dict
+
+import numpy as np
+
+from . import _native as nat
+from .api import _CODE, _is_torch
+
+VARIANTS = ("runs", "scan")
+
+
+def set_tile_pass(name: str) -> str:
+    """Select the calling thread's tile pass: "auto", "runs" or "scan".
+    Returns the previous setting."""
+    lib = nat.load()
+    prev = lib.cc3d_gpu_set_tile_pass(nat.TILE_PASSES[name])
+    if prev < 0:
+        nat.check(prev)
+    return {v: k for k, v in nat.TILE_PASSES.items()}[prev]
+
+
+def _volume(data: Any):
+    """(pointer, dtype code, sx, sy, sz, mem flags, stream, keepalive) of a numpy
+    array or CUDA tensor, as the labelling entry points see it."""
+    if _is_torch(data) and data.is_cuda:
+        import torch
+        t = data.contiguous()
+        npd = np.dtype(str(t.dtype).replace("torch.", ""))
+        if npd == np.float16:
+            t, npd = t.view(torch.int16), np.dtype(np.uint16)
+        npd = {np.dtype(np.int8): np.dtype(np.uint8), np.dtype(np.int16): np.dtype(np.uint16),
+               np.dtype(np.int32): np.dtype(np.uint32), np.dtype(np.int64): np.dtype(np.uint64),
+               np.dtype(np.bool_): np.dtype(np.uint8)}.get(npd, npd)
+        shape = list(t.shape)
+        ptr, mem = t.data_ptr(), nat.IN_DEVICE
+        stream = ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+        keep = t
+    else:
+        a = np.ascontiguousarray(data.cpu().numpy() if _is_torch(data) else data)
+        if a.dtype == np.float16:
+            a = a.view(np.uint16)
+        if a.dtype.kind in "ib":
+            a = a.view({1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize])
+        npd, shape, ptr, mem, stream, keep = a.dtype, list(a.shape), a.ctypes.data, 0, None, a
+    if npd not in _CODE:
+        raise TypeError(f"unsupported dtype {npd}")
+    while len(shape) < 3:
+        shape.insert(0, 1)
+    sz, sy, sx = (int(v) for v in shape)
+    return ptr, _CODE[npd], sx, sy, sz, mem, stream, keep
+
+
+def tile_pass_choice(data: Any, connectivity: int = 26, binary_image: bool = False) -> str:
+    """The variant a labelling of `data` would use now."""
+    ptr, code, sx, sy, sz, mem, stream, keep = _volume(data)
+    v = nat.load().cc3d_gpu_tile_pass_choice(code, sx, sy, sz, int(connectivity), int(bool(binary_image)))
+    return VARIANTS[v - 1]
+
+
+def autotune(data: Any, connectivity: int = 26, binary_image: bool = False, repeats: int = 2) -> Dict[str, Any]:
+    """Time every tile-pass variant on `data` and record the faster one for its
+    class.  Returns {"best": name, "ms": {name: milliseconds}}."""
+    ptr, code, sx, sy, sz, mem, stream, keep = _volume(data)
+    best = ctypes.c_int(0)
+    ms = (ctypes.c_double * 2)()
+    nat.check(nat.load().cc3d_gpu_autotune(ptr, code, sx, sy, sz, int(connectivity), int(bool(binary_image)),
+                                           mem, stream, int(repeats), ctypes.byref(best), ms))
+    return {"best": VARIANTS[best.value - 1], "ms": {VARIANTS[i]: ms[i] for i in range(2)}}
+
+
+def autotune_reset() -> None:
+    """Forget every recorded choice."""
+    nat.load().cc3d_gpu_autotune_reset()

@@ -5,12 +5,14 @@
 // arguments like the reference's C++ entry points, stages host buffers, runs
 // the kernel pipeline on the caller's stream and maps device error words to
 // return codes.  No C++ exception crosses the ABI.
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include "cc3d_gpu.h"
 #include "cc3d_internal.h"
@@ -214,6 +216,31 @@ struct StageTimer {
 
 }  // namespace
 
+// ------------------------------------------------------------ tile-pass choice
+// The variant a thread asked for (CC3D_TILE_AUTO: the autotuner's choice for
+// the volume's class, else the default), and the autotuner's choices, shared
+// by all threads.  A class is (dtype, effective connectivity, relation mode,
+// size bucket of the voxel count).
+namespace {
+thread_local int g_tile_pass = CC3D_TILE_AUTO;
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tuned;
+
+int size_bucket(int64_t voxels) {
+  int b = 0;
+  while (voxels > 1 && b < 62) { voxels >>= 1; ++b; }
+  return b / 3;  // classes of 8x in voxel count
+}
+
+int resolve_tile_pass(int dtype, int eff, int mode, int64_t voxels) {
+  if (g_tile_pass != CC3D_TILE_AUTO) return g_tile_pass;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tuned.find(std::make_tuple(dtype, eff, mode, size_bucket(voxels)));
+  if (it != g_tuned.end()) return it->second;
+  return CC3D_TILE_RUNS;
+}
+}  // namespace
+
 // error reporting shared with the other host translation units
 int cc3dgpu::api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int cc3dgpu::api_device_errors(unsigned err) { return check_device_errors(err); }
@@ -294,9 +321,20 @@ int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t
   return CC3D_OK;
 }
 
+static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                         int64_t connectivity, int periodic_boundary, int binary_image,
+                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant);
+
 int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                            int64_t connectivity, int periodic_boundary, int binary_image,
                            int mem_flags, void* stream, cc3d_gpu_prepared* info) {
+  return label_prepare(in, dtype, sx, sy, sz, connectivity, periodic_boundary, binary_image, mem_flags,
+                       stream, info, CC3D_TILE_AUTO);
+}
+
+static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                         int64_t connectivity, int periodic_boundary, int binary_image,
+                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant) {
   const size_t isz = dtype_size(dtype);
   if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
   if (sx < 0 || sy < 0 || sz < 0 || !info) return fail(CC3D_ERR_INVALID, "invalid arguments");
@@ -408,7 +446,8 @@ int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, in
     a.in = base + o_in;
     tm.mark(0);
   }
-  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, ntiles, s));
+  if (variant == CC3D_TILE_AUTO) variant = resolve_tile_pass(dtype, eff, mode, voxels);
+  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, variant, ntiles, s));
   tm.mark(2);
   CK(launch_merge_edges(a, s));
   tm.mark(3);
@@ -656,6 +695,65 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   }
   CK(cudaStreamSynchronize(s));
   return CC3D_OK;
+}
+
+int cc3d_gpu_set_tile_pass(int variant) {
+  if (variant != CC3D_TILE_AUTO && variant != CC3D_TILE_RUNS && variant != CC3D_TILE_SCAN)
+    return fail(CC3D_ERR_INVALID, "unknown tile pass %d", variant);
+  const int prev = g_tile_pass;
+  g_tile_pass = variant;
+  return prev;
+}
+
+int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz, int64_t connectivity,
+                              int binary_image) {
+  const int conn = (int)connectivity;
+  int eff = conn;
+  if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
+  if (sz == 1 && conn == 6) eff = 4;
+  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
+  if (binary_image && conn == 8) return CC3D_TILE_RUNS;
+  return resolve_tile_pass(dtype, eff, mode, sx * sy * sz);
+}
+
+int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz, int64_t connectivity,
+                      int binary_image, int mem_flags, void* stream, int repeats, int* best,
+                      double* ms) {
+  if (!best) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  if (repeats < 1) repeats = 1;
+  const int variants[2] = {CC3D_TILE_RUNS, CC3D_TILE_SCAN};
+  double t[2] = {0, 0};
+  for (int v = 0; v < 2; ++v) {
+    double bestt = 1e300;
+    for (int r = 0; r < repeats + 1; ++r) {  // the first run warms up
+      cc3d_gpu_prepared info;
+      const auto t0 = std::chrono::steady_clock::now();
+      if (int rc = label_prepare(in, dtype, sx, sy, sz, connectivity, 0, binary_image, mem_flags, stream,
+                                 &info, variants[v]))
+        return rc;
+      const double dt = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (r > 0 && dt < bestt) bestt = dt;
+    }
+    t[v] = bestt;
+  }
+  const int conn = (int)connectivity;
+  int eff = conn;
+  if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
+  if (sz == 1 && conn == 6) eff = 4;
+  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
+  const int choice = t[1] < t[0] ? CC3D_TILE_SCAN : CC3D_TILE_RUNS;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[std::make_tuple(dtype, eff, mode, size_bucket(sx * sy * sz))] = choice;
+  }
+  *best = choice;
+  if (ms) { ms[0] = t[0]; ms[1] = t[1]; }
+  return CC3D_OK;
+}
+
+void cc3d_gpu_autotune_reset(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned.clear();
 }
 
 }  // extern "C"

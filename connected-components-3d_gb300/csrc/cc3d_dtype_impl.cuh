@@ -176,7 +176,7 @@ constexpr CUtensorMapDataType tma_type() {
 // 16-byte aligned base and rows whose byte length is a multiple of 16 (the
 // copy engine's stride rule).  Otherwise the warps load the rows themselves.
 template <typename T, int CONN, int TY, int TZ, int MODE>
-cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+cudaError_t launch_k1_scan(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   using G = ScanGeom<T, CONN, TY, TZ>;
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
@@ -204,39 +204,46 @@ cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// binary 8-connected images are numbered by 2x2 blocks: the block-parallel pass
-template <typename T>
-cudaError_t launch_k1_block8(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  k_tile_runs<T, 8, 64, 1, MODE_BINARY, true><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+// the block-parallel pass: one CTA of 256 threads per tile
+template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
+cudaError_t launch_k1_runs(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  k_tile_runs<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
+template <typename T, int CONN, int TY, int TZ, int MODE>
+cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, int variant, cudaStream_t s) {
+  if (variant == TILE_PASS_RUNS) return launch_k1_runs<T, CONN, TY, TZ, MODE, false>(a, ntiles, s);
+  if (variant == TILE_PASS_SCAN) return launch_k1_scan<T, CONN, TY, TZ, MODE>(a, ntiles, s);
+  return cudaErrorInvalidValue;
+}
+
 template <typename T>
-cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool block8,
+cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool block8, int variant,
                                 int64_t ntiles, cudaStream_t s) {
+  const bool d3 = conn == 26 || conn == 18 || conn == 6;
+  if (d3 && (a.ty != 8 || a.tz != 8)) return cudaErrorInvalidValue;
+  if (!d3 && (a.ty != 64 || a.tz != 1)) return cudaErrorInvalidValue;
+  const bool multi = mode == MODE_MULTI;
   switch (conn) {
     case 26:
-      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 26, 8, 8, MODE_MULTI>(a, ntiles, s)
-                                : launch_k1<T, 26, 8, 8, MODE_BINARY>(a, ntiles, s);
+      return multi ? launch_k1<T, 26, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1<T, 26, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
     case 18:
-      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 18, 8, 8, MODE_MULTI>(a, ntiles, s)
-                                : launch_k1<T, 18, 8, 8, MODE_BINARY>(a, ntiles, s);
+      return multi ? launch_k1<T, 18, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1<T, 18, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
     case 6:
-      if (a.ty != 8 || a.tz != 8) return cudaErrorInvalidValue;
-      return mode == MODE_MULTI ? launch_k1<T, 6, 8, 8, MODE_MULTI>(a, ntiles, s)
-                                : launch_k1<T, 6, 8, 8, MODE_BINARY>(a, ntiles, s);
+      return multi ? launch_k1<T, 6, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1<T, 6, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
     case 8:
-      if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
-      if (mode == MODE_MULTI) return launch_k1<T, 8, 64, 1, MODE_MULTI>(a, ntiles, s);
-      if (block8) return launch_k1_block8<T>(a, ntiles, s);
-      return launch_k1<T, 8, 64, 1, MODE_BINARY>(a, ntiles, s);
+      // binary 8-connected images are numbered by 2x2 blocks: block-parallel pass only
+      if (block8) return launch_k1_runs<T, 8, 64, 1, MODE_BINARY, true>(a, ntiles, s);
+      return multi ? launch_k1<T, 8, 64, 1, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1<T, 8, 64, 1, MODE_BINARY>(a, ntiles, variant, s);
     case 4:
-      if (a.ty != 64 || a.tz != 1) return cudaErrorInvalidValue;
-      if (mode == MODE_MULTI) return launch_k1<T, 4, 64, 1, MODE_MULTI>(a, ntiles, s);
-      if (mode == MODE_BINARY4) return launch_k1<T, 4, 64, 1, MODE_BINARY4>(a, ntiles, s);
-      return launch_k1<T, 4, 64, 1, MODE_BINARY>(a, ntiles, s);
+      if (mode == MODE_BINARY4) return launch_k1<T, 4, 64, 1, MODE_BINARY4>(a, ntiles, variant, s);
+      return multi ? launch_k1<T, 4, 64, 1, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1<T, 4, 64, 1, MODE_BINARY>(a, ntiles, variant, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -291,8 +298,8 @@ cudaError_t launch_minmax_t(const void* in, int64_t n, int is_signed, unsigned l
 #define CC3D_DEFINE_DTYPE_LAUNCHERS(SUF, T)                                               \
   namespace cc3dgpu {                                                                     \
   cudaError_t launch_tile_local_##SUF(const LabelArgs& a, int conn, int mode, bool block8,  \
-                                      int64_t ntiles, cudaStream_t s) {                   \
-    return launch_tile_local_t<T>(a, conn, mode, block8, ntiles, s);                      \
+                                      int variant, int64_t ntiles, cudaStream_t s) {      \
+    return launch_tile_local_t<T>(a, conn, mode, block8, variant, ntiles, s);             \
   }                                                                                       \
   cudaError_t launch_wrap_##SUF(const LabelArgs& a, int conn, int mode, cudaStream_t s) { \
     return launch_wrap_t<T>(a, conn, mode, s);                                            \

@@ -13,9 +13,15 @@ namespace cc3dgpu {
 
 // per-dtype launchers of the tile labeller and the periodic wrap unions
 // (one translation unit per element type: label_<type>.cu)
+// tile-pass variants: the block-parallel pass (k_tile_runs) and the
+// warp-per-tile raster scan (k_tile_scan)
+constexpr int TILE_PASS_RUNS = 1;
+constexpr int TILE_PASS_SCAN = 2;
+
 #define CC3D_DECLARE_DTYPE_LAUNCHERS(SUF)                                              \
   cudaError_t launch_tile_local_##SUF(const LabelArgs& a, int conn, int mode,         \
-                                      bool block8, int64_t ntiles, cudaStream_t s);   \
+                                      bool block8, int variant, int64_t ntiles,        \
+                                      cudaStream_t s);                                 \
   cudaError_t launch_wrap_##SUF(const LabelArgs& a, int conn, int mode, cudaStream_t s); \
   cudaError_t launch_epl_##SUF(const void* in, int64_t sx, int64_t voxels,            \
                                Counters* ctr, cudaStream_t s);                        \

@@ -219,7 +219,8 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   h.last_row = -1;
   CKN(cudaMemcpyAsync(a.ctr, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   if (block8) CKN(cudaMemsetAsync(a.bitmap, 0, nwords * sizeof(uint32_t), s));
-  CKN(NOALLOC_DISPATCH(dtype, launch_tile_local, a, eff, mode, block8, ntiles, s));
+  CKN(NOALLOC_DISPATCH(dtype, launch_tile_local, a, eff, mode, block8,
+                       cc3d_gpu_tile_pass_choice(dtype, sx, sy, sz, connectivity, binary_image), ntiles, s));
   CKN(launch_merge_edges(a, s));
   if (periodic_boundary) CKN(NOALLOC_DISPATCH(dtype, launch_wrap, a, eff, mode, s));
   CKN(launch_scan(a, nwords, bsum, nblocks, s));

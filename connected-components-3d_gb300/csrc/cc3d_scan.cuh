@@ -90,11 +90,11 @@ struct ScanGeom {
   static constexpr int W = 32 + 2 * PADX;           // elements per loaded row
   // ring slot stride: TMA writes to 128-byte aligned shared memory
   static constexpr int SLOT = (int)(((CH * W * sizeof(T) + 127) / 128 * 128) / sizeof(T));
-  static constexpr int DB = D3 ? BY + 1 : 1;        // farthest backward row (dy = dz = -1 in 3D)
-  static constexpr int RL = 16;                     // label ring rows
+  // label slots: 3D keeps the previous and the current plane, 2D the
+  // previous and the current row
+  static constexpr int LS = D3 ? 2 * BY : 2;
   static constexpr int NHL = (NRB - TY * TZ) * 32 + 2 * NRB;  // halo labels
   static constexpr int NLAB = kTV + NHL;
-  static_assert(RL > DB, "label ring too short");
   static_assert(NLAB < (int)kCompFlag, "labels must leave the flag bit free");
 };
 
@@ -103,9 +103,9 @@ struct alignas(128) ScanSmem {
   using G = ScanGeom<T, CONN, TY, TZ>;
   T vals[G::NS][G::SLOT];
   uint64_t bar[G::NS];
-  uint16_t labr[G::RL][34];   // labels of recent rows; [0] = column x0-1, [33] = column x0+32
-  uint32_t fmr[G::RL];        // foreground masks of recent rows
-  uint32_t colfg[G::RL];      // bit 0: column x0-1 foreground, bit 1: column x0+32
+  uint16_t lab[G::LS][34];    // labels of recent rows; [0] = column x0-1, [33] = column x0+32
+  uint32_t fmr[G::LS];        // foreground masks of recent rows
+  uint32_t colfg[G::LS];      // bit 0: column x0-1 foreground, bit 1: column x0+32
   uint16_t par[G::NLAB];      // union-find over labels
   uint16_t hpos[G::NHL];      // halo label -> rb * 34 + i of the voxel that opened it
   uint16_t runlab[kTV];       // label of every tile run, in tile raster order
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kScanWarps * 32, 1)
 k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
   using G = ScanGeom<T, CONN, TY, TZ>;
   using SMem = ScanSmem<T, CONN, TY, TZ>;
-  constexpr int BY = G::BY, BZ = G::BZ, HZ = G::HZ, NRB = G::NRB, CH = G::CH, NS = G::NS;
+  constexpr int BY = G::BY, HZ = G::HZ, NRB = G::NRB, CH = G::CH, NS = G::NS;
   constexpr int NR = TY * TZ;
   constexpr int NRN = RowNb<CONN>::n;
   constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
@@ -162,14 +162,6 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     return;
   }
 
-  auto is_tile_row = [&](int rb) -> bool {
-    const int by = rb % BY, bz = rb / BY;
-    return by >= 1 && by <= TY && bz >= HZ;
-  };
-  auto row_owner = [&](int rb) -> int {
-    const int by = rb % BY, bz = rb / BY;
-    return (by == 0 ? 0 : (by == BY - 1 ? 2 : 1)) + 3 * (bz < HZ ? 0 : 1);
-  };
   auto find = [&](uint16_t n) -> uint16_t { return sfind(sm.par, n); };
 
   // ---- ring of chunks: chunk c holds box rows [c * CH, c * CH + CH)
@@ -223,43 +215,53 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   unsigned long long epl_acc = 0;
   long long frow = 0x7FFFFFFFFFFFFFFFLL, lrow = -1;
   uint32_t prov = 0;
-  // values and labels of box row r by column i (0 = x0 - 1, 1..32 = the tile's
-  // columns, 33 = x0 + 32)
-  auto vrow = [&](int r) -> const T* { return &sm.vals[(r / CH) % NS][(r % CH) * G::W + G::PADX - 1]; };
-  auto lrow_of = [&](int r) -> uint16_t* { return sm.labr[r % G::RL]; };
+  // Box row (by, bz) = rb: its values by column i (0 = x0 - 1, 1..32 = the
+  // tile's columns, 33 = x0 + 32) and its label slot.  3D chunks are whole
+  // planes, so a row's chunk is its plane.
+  auto vrow = [&](int r, int by_, int bz_) -> const T* {
+    if (G::D3) return &sm.vals[bz_ % NS][by_ * G::W + G::PADX - 1];
+    return &sm.vals[(r / CH) % NS][(r % CH) * G::W + G::PADX - 1];
+  };
+  auto lslot = [&](int r, int by_, int bz_) -> int { return G::D3 ? (bz_ & 1) * BY + by_ : (r & 1); };
+  auto owner_of = [&](int by_, int bz_) -> int {
+    return (by_ == 0 ? 0 : (by_ == BY - 1 ? 2 : 1)) + 3 * (bz_ < HZ ? 0 : 1);
+  };
   constexpr int NC = 2 * NRN + 1;  // candidate slots of a voxel
 
   issue(0);
-  for (int c = 0; c < G::NCH; ++c) {
-    wait(c);
-    if (err & ERR_WAIT) break;  // a chunk that never arrived: report, start no more copies
-    issue(c + 1);
-    const int rend = (c + 1) * CH < NRB ? (c + 1) * CH : NRB;
-    for (int rb = c * CH; rb < rend; ++rb) {
-      const int by = rb % BY, bz = rb / BY;
+  int by = 0, bz = 0;
+  for (int rb = 0; rb < NRB; ++rb) {
+    if (rb % CH == 0) {
+      const int c = rb / CH;
+      wait(c);
+      if (err & ERR_WAIT) break;  // a chunk that never arrived: report, start no more copies
+      issue(c + 1);
+    }
+    {
       const bool trow = by >= 1 && by <= TY && bz >= HZ;
-      const int own = row_owner(rb);
-      const T* vc = vrow(rb);
-      uint16_t* lc = lrow_of(rb);
+      const int own = owner_of(by, bz);
+      const T* vc = vrow(rb, by, bz);
+      const int ls = lslot(rb, by, bz);
+      uint16_t* lc = sm.lab[ls];
       // backward neighbour rows (warp-uniform); grp: a halo or column voxel of
       // this row may group with that row (dx = 0, inside the box, same owner)
       const T* vn[NRN];
       const uint16_t* ln[NRN];
       bool grp[NRN], grp_row[NRN];
-      int rbn[NRN];
+      int lsn[NRN];
 #pragma unroll
       for (int k = 0; k < NRN; ++k) {
         int dy, dz, dxs;
         row_nb<CONN>(k, dy, dz, dxs);
         const int byp = by + dy, bzp = bz + dz;
-        const bool inbox = byp >= 0 && byp < BY && bzp >= 0 && bzp < BZ;
-        rbn[k] = inbox ? rb + dy + BY * dz : rb;
-        vn[k] = vrow(rbn[k]);
-        ln[k] = lrow_of(rbn[k]);
-        grp[k] = inbox && (dxs & 2) && row_owner(rbn[k]) == own;
-        grp_row[k] = grp[k] && !is_tile_row(rbn[k]);
+        const bool inbox = byp >= 0 && byp < BY && bzp >= 0;
+        const int byq = inbox ? byp : by, bzq = inbox ? bzp : bz;
+        vn[k] = vrow(rb + (inbox ? dy + BY * dz : 0), byq, bzq);
+        lsn[k] = lslot(rb + (inbox ? dy + BY * dz : 0), byq, bzq);
+        ln[k] = sm.lab[lsn[k]];
+        grp[k] = inbox && (dxs & 2) && owner_of(byp, bzp) == own;
+        grp_row[k] = grp[k] && !(byp >= 1 && byp <= TY && bzp >= HZ);
       }
-
       // -- the two halo columns of this row (lanes 0 and 1)
       {
         const int ci = lane == 0 ? 0 : 33;
@@ -299,7 +301,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         }
         hl += __popc(nm);
         if (lane < 2) lc[ci] = (uint16_t)clab;
-        if (lane == 0) sm.colfg[rb % G::RL] = (is_fg(vc[0]) ? 1u : 0u) | (is_fg(vc[33]) ? 2u : 0u);
+        if (lane == 0) sm.colfg[ls] = (is_fg(vc[0]) ? 1u : 0u) | (is_fg(vc[33]) ? 2u : 0u);
       }
       __syncwarp();
 
@@ -428,7 +430,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         if (needmerge && !sunite(sm.par, RL, (uint16_t)c1)) err |= ERR_LOCAL_BUDGET;
       }
       lc[lane + 1] = fg ? RL : kNoLabel;
-      if (lane == 0) sm.fmr[rb % G::RL] = F;
+      if (lane == 0) sm.fmr[ls] = F;
 
       if (trow) {
         const int ri = (by - 1) + TY * (bz - HZ);
@@ -458,13 +460,13 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
             const T prev = lane == 0 ? vc[0] : sl;
             Lk = __ballot_sync(FULL, fg && is_fg(prev) && v == prev);
           } else {
-            Lk = (F << 1) | (sm.colfg[rb % G::RL] & 1u);
+            Lk = (F << 1) | (sm.colfg[ls] & 1u);
           }
 #pragma unroll
           for (int k = 0; k < NRN; ++k) {
             int dy, dz, dxs;
             row_nb<CONN>(k, dy, dz, dxs);
-            const uint32_t Fp = sm.fmr[rbn[k] % G::RL], cf = sm.colfg[rbn[k] % G::RL];
+            const uint32_t Fp = sm.fmr[lsn[k]], cf = sm.colfg[lsn[k]];
             if (dxs & 2) Lk |= Fp;
             if (dxs & 1) Lk |= (Fp << 1) | (cf & 1u);
             if (dxs & 4) Lk |= (Fp >> 1) | ((cf & 2u) ? 0x80000000u : 0u);
@@ -473,6 +475,10 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         }
       }
       __syncwarp();
+    }
+    if (++by == BY) {
+      by = 0;
+      ++bz;
     }
   }
 

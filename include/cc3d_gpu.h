@@ -186,6 +186,40 @@ int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
 void cc3d_gpu_release_workspace(void);
 
 /*
+ * Tile-pass variants and their autotuner.  No counterpart in the reference,
+ * which has a single CPU algorithm per connectivity.  Every variant gives
+ * identical labels; they differ only in speed:
+ *   CC3D_TILE_RUNS  one 256-thread block per 32x8x8 (3D) / 32x64 (2D) tile:
+ *                   rows cut into runs by ballots, unions of overlapping runs
+ *                   in a shared-memory union-find.
+ *   CC3D_TILE_SCAN  one warp per tile scanning its rows in raster order,
+ *                   fed by TMA: runs copy the root of their backward
+ *                   neighbours; unions only where two labels meet.
+ * Binary 8-connected images always use CC3D_TILE_RUNS (2x2-block numbering).
+ *
+ * cc3d_gpu_set_tile_pass: the calling thread's choice (CC3D_TILE_AUTO = the
+ *   autotuned choice for the volume's class, else CC3D_TILE_RUNS); returns
+ *   the previous setting.
+ * cc3d_gpu_tile_pass_choice: the variant a labelling of this volume would use.
+ * cc3d_gpu_autotune: times every variant on `in` (best of `repeats` after one
+ *   warm-up run each), records the faster one for the volume's class (dtype,
+ *   effective connectivity, binary or not, voxel count within a factor of 8)
+ *   and returns it in *best, with the milliseconds of each variant in
+ *   ms[0] (RUNS) and ms[1] (SCAN) when ms is not NULL.
+ * cc3d_gpu_autotune_reset: forget every recorded choice.
+ */
+#define CC3D_TILE_AUTO 0
+#define CC3D_TILE_RUNS 1
+#define CC3D_TILE_SCAN 2
+int cc3d_gpu_set_tile_pass(int variant);
+int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz,
+                              int64_t connectivity, int binary_image);
+int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                      int64_t connectivity, int binary_image, int mem_flags, void* stream,
+                      int repeats, int* best, double* ms);
+void cc3d_gpu_autotune_reset(void);
+
+/*
  * Labelling that allocates nothing.  No counterpart in the reference: the
  * reference labels on the CPU into a buffer its caller allocated and needs no
  * device scratch.

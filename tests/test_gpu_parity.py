@@ -11,12 +11,17 @@ import __graft_entry__ as entry
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def cc3d():
+@pytest.fixture(scope="module", params=["runs", "scan"])
+def cc3d(request):
+    """The package with one tile-pass variant selected: every parity test runs
+    once per variant."""
     entry.build()
     import torch
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
-    return entry.package()
+    pkg = entry.package()
+    prev = pkg.set_tile_pass(request.param)
+    yield pkg
+    pkg.set_tile_pass(prev)
 
 
 def _on_device(fn):

@@ -1,0 +1,60 @@
+"""Tile-pass variants and the autotuner (cc3d_gpu_set_tile_pass,
+cc3d_gpu_tile_pass_choice, cc3d_gpu_autotune).  The choice itself needs no GPU;
+timing the variants does."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as entry
+
+
+@pytest.fixture(scope="module")
+def cc3d():
+    entry.build()
+    pkg = entry.package()
+    yield pkg
+    pkg.set_tile_pass("auto")
+    pkg.autotune_reset()
+
+
+def test_choice_follows_the_thread_setting(cc3d):
+    vol = np.zeros((40, 50, 60), np.uint32)
+    assert cc3d.set_tile_pass("scan") == "auto"
+    assert cc3d.tile_pass_choice(vol) == "scan"
+    assert cc3d.set_tile_pass("runs") == "scan"
+    assert cc3d.tile_pass_choice(vol) == "runs"
+    cc3d.set_tile_pass("auto")
+    cc3d.autotune_reset()
+    assert cc3d.tile_pass_choice(vol) == "runs"  # the default without tuning data
+    # binary 8-connected images always take the block pass (2x2-block numbering)
+    cc3d.set_tile_pass("scan")
+    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs"
+    cc3d.set_tile_pass("auto")
+
+
+def test_unknown_variant_is_rejected(cc3d):
+    lib = cc3d._native.load()
+    assert lib.cc3d_gpu_set_tile_pass(7) == -1
+    with pytest.raises(KeyError):
+        cc3d.set_tile_pass("fastest")
+
+
+@pytest.mark.gpu
+def test_autotune_records_the_faster_variant(cc3d):
+    import torch
+    from cc3d_gb300 import synth
+    vol = synth.voronoi_volume((96, 128, 160), 200, 1 << 20, seed=21)
+    cc3d.autotune_reset()
+    for data in (vol, torch.from_numpy(vol).cuda()):
+        res = cc3d.autotune(data, connectivity=26)
+        assert res["best"] in ("runs", "scan")
+        assert all(ms > 0 for ms in res["ms"].values())
+        assert res["best"] == min(res["ms"], key=res["ms"].get)
+        assert cc3d.tile_pass_choice(vol, connectivity=26) == res["best"]
+        # the labels do not depend on the choice
+        out, N = cc3d.connected_components(data, connectivity=26, return_N=True)
+        cc3d.set_tile_pass("runs" if res["best"] == "scan" else "scan")
+        out2, N2 = cc3d.connected_components(data, connectivity=26, return_N=True)
+        cc3d.set_tile_pass("auto")
+        assert N == N2
+        assert np.array_equal(np.asarray(out.cpu() if hasattr(out, "cpu") else out),
+                              np.asarray(out2.cpu() if hasattr(out2, "cpu") else out2))
