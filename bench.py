@@ -18,7 +18,8 @@ write of the uint32 output.  Inputs are synthetic and seeded.
 --impl reference
     The reference's CPU implementation of the path on this machine's host
     cores: the compiled reference where it was built here (oracle/_ref), else
-    the oracle's C restatement.  It is single-threaded.
+    the oracle's C restatement.  It is single-threaded, so each step labels
+    one copy of the volume per core in parallel processes.
 
 Multi-GPU (torchrun): every rank labels its own volume (replicas; the
 path has no data exchange), value = all voxels / max over ranks of the time.
@@ -160,31 +161,66 @@ def cpu_reference(vol: np.ndarray, budget_s: float = 20.0):
                       f"({best:.3f} s per volume, N={N})"}
 
 
+_REF_VOLUME = None
+
+
+def _ref_worker_init(path: str) -> None:
+    global _REF_VOLUME
+    _REF_VOLUME = np.load(path, mmap_mode="r")
+
+
+def _ref_worker_label(_: int):
+    """One labelling of the workload volume by the reference's CPU path (the
+    compiled reference where present, else the oracle port); returns seconds."""
+    import oracle
+    kind = "reference" if oracle.have_reference() else "port"
+    vol = np.ascontiguousarray(_REF_VOLUME)
+    t0 = time.perf_counter()
+    _, n = oracle.connected_components(vol, connectivity=CONN, return_N=True, backend=kind)
+    return time.perf_counter() - t0, int(n)
+
+
 def run_reference(args, world, rank):
+    """The reference's CPU implementation on all host cores: the reference is
+    single-threaded, so every step labels one copy of the workload volume per
+    core, in parallel processes (spawned before any GPU use).  value = voxels
+    labelled by all cores / wall time of the step."""
     if rank != 0:
         return
-    vol = make_volume(0)
-    times = []
+    import multiprocessing as mp
+    import tempfile
     import oracle
     oracle.build()
     kind = "reference" if oracle.have_reference() else "port"
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        _, N = oracle.connected_components(vol, connectivity=CONN, return_N=True, backend=kind)
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
+    vol = make_volume(0)
+    cores = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+    shm = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    with tempfile.TemporaryDirectory(dir=shm) as tmp:
+        path = os.path.join(tmp, "volume.npy")
+        np.save(path, vol)
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores, initializer=_ref_worker_init, initargs=(path,)) as pool:
+            times = []
+            for i in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                res = pool.map(_ref_worker_label, range(cores), chunksize=1)
+                dt = time.perf_counter() - t0
+                if i >= args.warmup:
+                    times.append(dt)
     ms = 1000.0 * sum(times) / len(times)
-    value = vol.size / (ms / 1000.0) / 1e9
+    value = cores * vol.size / (ms / 1000.0) / 1e9
+    per_volume_s = float(np.median([r[0] for r in res]))
     line = {
         "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded Voronoi)",
-        "config": {"workload": "512^3 uint32 Voronoi(4096 seeds)+membrane+2% salt, connectivity 26",
-                   "volumes_per_step": 1, "l2": "input larger than L2"},
+        "config": {"workload": "512^3 uint32 Voronoi(4096 seeds, labels in [1,2^20])+membrane+2% salt, "
+                               "connectivity 26, output uint32",
+                   "volumes_per_step": cores, "l2": "input larger than L2"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "GVoxels/s", "cores": 1, "kind": kind,
-                         "sample": "the full 512^3 volume per step (single-threaded CPU code)"},
+        "cpu_baseline": {"value": value, "unit": "GVoxels/s", "cores": cores, "kind": kind,
+                         "sample": f"{cores} copies of the full 512^3 volume per step, one per core in "
+                                   f"parallel processes ({per_volume_s:.3f} s per volume, N={res[0][1]})"},
         "e2e": {"value": value, "unit": "GVoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -197,6 +233,7 @@ def run_gpu(args, world, rank, local):
     cc3d.build()
     nat = cc3d._native
     lib = nat.load()
+    cc3d.set_tile_pass(args.tile_pass)
 
     vol = make_volume(rank)
     voxels = vol.size
@@ -363,7 +400,8 @@ def run_all_configs(args):
             cache[key] = torch.from_numpy(make()).cuda()
         dev = cache[key]
         res = {}
-        for variant in ("runs", "scan", "auto"):
+        from cc3d_gb300.tuning import CONFIGS
+        for variant in CONFIGS + ("auto",):
             if variant == "auto":
                 cc3d.set_tile_pass("auto")
                 tuned = cc3d.autotune(dev, connectivity=kw["connectivity"],
@@ -386,6 +424,113 @@ def run_all_configs(args):
                           "variants": res}), flush=True)
 
 
+# ------------------------------------------------------------ batched stream
+def run_batch(args):
+    """The mixed-size stream: N uint16 Voronoi+membrane volumes, every edge
+    log-uniform in [16, 256], one seed per 4096 voxels, labels in [1, 65535],
+    26-connectivity.  One JSON line: the batched path (one launch per stage,
+    replayed CUDA graph, tile pass from the batch autotuner) against one
+    connected_components call per volume, and the oracle's CPU loop on a
+    bounded sample.  Every batched volume is checked against its
+    single-volume result."""
+    import torch
+    import cc3d_gb300 as cc3d
+    from cc3d_gb300 import synth
+    cc3d.build()
+    shapes = synth.batch_shapes(args.batch, 16, 256, seed=12)
+    t0 = time.perf_counter()
+    vols = [synth.voronoi_volume(s, max(1, int(np.prod(s)) // 4096), 65535, seed=100 + i, dtype=np.uint16,
+                                 salt=0.0) for i, s in enumerate(shapes)]
+    t_gen = time.perf_counter() - t0
+    voxels = int(sum(v.size for v in vols))
+    dev = [torch.from_numpy(v).cuda() for v in vols]
+    tuned = cc3d.autotune_batch(dev, connectivity=26)
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_batch = timed(lambda: cc3d.connected_components_batch(dev, connectivity=26), args.steps)
+    ms_loop = timed(lambda: [cc3d.connected_components(d, connectivity=26) for d in dev], max(1, args.steps // 3))
+    # every volume: batched == single-volume path
+    got = cc3d.connected_components_batch(dev, connectivity=26, return_N=True)
+    mismatches = 0
+    for d, (lab, n) in zip(dev, got):
+        ref, rn = cc3d.connected_components(d, connectivity=26, return_N=True)
+        mismatches += int(rn != n or ref.dtype != lab.dtype or not torch.equal(ref.to(torch.int64), lab.to(torch.int64)))
+    cpu = None
+    if not args.skip_cpu:
+        import oracle
+        oracle.build()
+        kind = "reference" if oracle.have_reference() else "port"
+        done, t_cpu, t0 = 0, 0.0, time.perf_counter()
+        k = 0
+        while k < len(vols) and time.perf_counter() - t0 < 20.0:
+            t1 = time.perf_counter()
+            oracle.connected_components(vols[k], connectivity=26, backend=kind)
+            t_cpu += time.perf_counter() - t1
+            done += vols[k].size
+            k += 1
+        cpu = {"value": done / t_cpu / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": kind,
+               "sample": f"the first {k} volumes of the stream ({done} voxels), one after another"}
+    print(json.dumps({
+        "metric": "GVoxels/s mixed-size stream, batched vs per-volume (bit-exact)",
+        "value": voxels / ms_batch / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_batch,
+        "per_volume_loop": {"value": voxels / ms_loop / 1e6, "ms_per_step": ms_loop},
+        "speedup_vs_per_volume": ms_loop / ms_batch,
+        "tuned": tuned, "mismatched_volumes": mismatches, "cpu_baseline": cpu,
+        "config": {"workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], "
+                               "one seed per 4096 voxels, connectivity 26",
+                   "voxels": voxels, "generation_s": t_gen},
+    }), flush=True)
+
+
+# ------------------------------------------------------------ cost model
+def run_costmodel(args):
+    """Train the cost model on autotuner timings of `args.costmodel` generated
+    volumes (Voronoi with 1 to ~1e6 seeds, Bernoulli p 0.05-0.95, multilabel
+    Bernoulli K 2-1000; uint8/16/32/64; edges 64-320; connectivity 26/18/6)
+    and judge it on a held-out-seed stream by its regret against the
+    exhaustive autotuner.  One JSON line; the parameters are saved where
+    --save-params says (and loaded by set_tile_pass("model") when shipped in
+    the package)."""
+    import torch
+    import cc3d_gb300 as cc3d
+    cm = cc3d.costmodel
+    cc3d.build()
+    t0 = time.perf_counter()
+    X, Y, _ = cm.collect(args.costmodel, seed=1)
+    t_collect = time.perf_counter() - t0
+    loss = cm.train(X, Y, epochs=300, batch=256, lr=1e-3, seed=0)
+    t_train = time.perf_counter() - t0 - t_collect
+    n_test = max(50, args.costmodel // 5)
+    Xt, Yt, desc = cm.collect(n_test, seed=2)
+    P = cm.predict(Xt)
+    reg = cm.regret(Yt, P)
+    srt = np.sort(np.where(np.isnan(Yt), np.inf, P), axis=1)
+    low_conf = float(np.mean(srt[:, 1] - srt[:, 0] < np.log1p(0.05)))
+    if args.save_params:
+        os.makedirs(os.path.dirname(os.path.abspath(args.save_params)), exist_ok=True)
+        cm.save(args.save_params)
+    print(json.dumps({
+        "metric": "cost-model regret vs exhaustive autotuner (held-out seeds)",
+        "value": reg["mean_regret"], "unit": "fraction slower than the best configuration",
+        "higher_is_better": False, "regret": reg, "low_confidence_fraction": low_conf,
+        "train": {"volumes": int(X.shape[0]), "timings": int(np.isfinite(Y).sum()), "final_loss": loss,
+                  "collect_s": t_collect, "train_s": t_train},
+        "test": {"volumes": int(Xt.shape[0]), "timings": int(np.isfinite(Yt).sum())},
+        "model": "FP32 MLP 16-64-64-6 (ReLU), Adam, trained by the library's CUDA kernels",
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,6 +542,14 @@ def main():
     ap.add_argument("--size", type=int, default=512, help="cube edge (profiling captures only)")
     ap.add_argument("--all-configs", action="store_true",
                     help="one line per benchmarked workload and tile-pass variant instead of the headline")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="the mixed-size stream of this many volumes instead of the headline")
+    ap.add_argument("--costmodel", type=int, default=0,
+                    help="train and judge the cost model on this many generated volumes instead of the headline")
+    ap.add_argument("--save-params", default="", help="where --costmodel saves the trained parameters")
+    ap.add_argument("--tile-pass", default="auto",
+                    help="tile-pass configuration of the headline run: auto, runs, scan or "
+                         "<variant>/<shape> (profiling captures)")
     args = ap.parse_args()
     global SHAPE, N_SEEDS
     if args.size != 512:
@@ -406,6 +559,12 @@ def main():
         args.warmup = 3
     if args.all_configs:
         run_all_configs(args)
+        return
+    if args.batch:
+        run_batch(args)
+        return
+    if args.costmodel:
+        run_costmodel(args)
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -13,6 +13,8 @@ from .api import (  # noqa: F401
 )
 from . import _native  # noqa: F401
 from .tuning import autotune, autotune_reset, set_tile_pass, tile_pass_choice  # noqa: F401
+from .batch import autotune_batch, connected_components_batch  # noqa: F401
+from . import costmodel, tuning  # noqa: F401
 
 __all__ = [
     "build",
@@ -20,6 +22,8 @@ __all__ = [
     "estimate_provisional_labels",
     "statistics",
     "DimensionError",
+    "connected_components_batch",
+    "autotune_batch",
     "autotune",
     "autotune_reset",
     "set_tile_pass",

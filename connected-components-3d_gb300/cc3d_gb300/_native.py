@@ -40,10 +40,19 @@ EXPORTED = (
     "cc3d_gpu_connected_components3d_noalloc",
     "cc3d_gpu_set_tile_pass",
     "cc3d_gpu_tile_pass_choice",
+    "cc3d_gpu_tile_config",
     "cc3d_gpu_autotune",
     "cc3d_gpu_autotune_reset",
+    "cc3d_gpu_label_batch",
+    "cc3d_gpu_release_batch",
+    "cc3d_gpu_autotune_batch",
+    "cc3d_gpu_volume_features",
+    "cc3d_gpu_cost_model_train",
+    "cc3d_gpu_cost_model_predict",
+    "cc3d_gpu_cost_model_get",
+    "cc3d_gpu_cost_model_set",
+    "cc3d_gpu_cost_model_choose",
 )
-TILE_PASSES = {"auto": 0, "runs": 1, "scan": 2}
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
 
 class Prepared(ctypes.Structure):
@@ -96,11 +105,31 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_set_tile_pass.restype = ci
         lib.cc3d_gpu_tile_pass_choice.argtypes = [ci, i64, i64, i64, i64, ci]
         lib.cc3d_gpu_tile_pass_choice.restype = ci
+        lib.cc3d_gpu_tile_config.argtypes = [ci]
+        lib.cc3d_gpu_tile_config.restype = ci
         lib.cc3d_gpu_autotune.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, ci,
                                           ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_double)]
         lib.cc3d_gpu_autotune.restype = ci
         lib.cc3d_gpu_autotune_reset.argtypes = []
         lib.cc3d_gpu_autotune_reset.restype = None
+        lib.cc3d_gpu_label_batch.argtypes = [vp, ci, ci, i64, vp, vp]
+        lib.cc3d_gpu_label_batch.restype = ci
+        lib.cc3d_gpu_release_batch.argtypes = []
+        lib.cc3d_gpu_release_batch.restype = None
+        lib.cc3d_gpu_autotune_batch.argtypes = [vp, ci, ci, i64, vp, vp, ci, ctypes.POINTER(ci),
+                                                ctypes.POINTER(ctypes.c_double)]
+        lib.cc3d_gpu_autotune_batch.restype = ci
+        fp = ctypes.POINTER(ctypes.c_float)
+        lib.cc3d_gpu_volume_features.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, fp]
+        lib.cc3d_gpu_cost_model_train.argtypes = [vp, vp, ci, ci, ci, ctypes.c_float, ctypes.c_uint64, fp]
+        lib.cc3d_gpu_cost_model_predict.argtypes = [vp, ci, vp]
+        lib.cc3d_gpu_cost_model_get.argtypes = [vp, ci]
+        lib.cc3d_gpu_cost_model_set.argtypes = [vp, ci]
+        lib.cc3d_gpu_cost_model_choose.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, ctypes.c_float,
+                                                   ctypes.POINTER(ci), ctypes.POINTER(ci)]
+        for name in ("cc3d_gpu_volume_features", "cc3d_gpu_cost_model_train", "cc3d_gpu_cost_model_predict",
+                     "cc3d_gpu_cost_model_get", "cc3d_gpu_cost_model_set", "cc3d_gpu_cost_model_choose"):
+            getattr(lib, name).restype = ci
         lib.cc3d_gpu_profile_enable.argtypes = [ci]
         lib.cc3d_gpu_profile_enable.restype = None
         lib.cc3d_gpu_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), u64p, ci]

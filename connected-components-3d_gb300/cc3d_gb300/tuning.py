@@ -18,16 +18,46 @@ from . import _native as nat
 from .api import _CODE, _is_torch
 
 VARIANTS = ("runs", "scan")
+SHAPES = ("8x8", "4x16", "16x4")   # 3D tiles 32 x TY x TZ; 2D images always use 32 x 64
+_SHAPE_BITS = {"8x8": 0x00, "4x16": 0x10, "16x4": 0x20}
+# configuration index -> name, in the order of cc3d_gpu_tile_config
+CONFIGS = tuple(f"{v}/{s}" for s in SHAPES for v in VARIANTS)
+
+
+def config_code(name: str) -> int:
+    """CC3D_TILE_* code of "auto", "model", "runs", "scan" or "<variant>/<shape>"."""
+    if name == "auto":
+        return 0
+    if name == "model":
+        return 3
+    variant, _, shape = name.partition("/")
+    return {"runs": 1, "scan": 2}[variant] | _SHAPE_BITS[shape or "8x8"]
+
+
+def config_name(code: int) -> str:
+    if code == 0:
+        return "auto"
+    if code == 3:
+        return "model"
+    return f"{VARIANTS[(code & 15) - 1]}/{SHAPES[(code >> 4) & 15]}"
 
 
 def set_tile_pass(name: str) -> str:
-    """Select the calling thread's tile pass: "auto", "runs" or "scan".
+    """Select the calling thread's tile-pass configuration: "auto", "runs",
+    "scan" (32x8x8 tiles) or "<variant>/<shape>" such as "scan/4x16".
+    "model" lets the learned cost model choose per volume (the parameters
+    shipped with the package are loaded if no model was trained or loaded).
     Returns the previous setting."""
-    lib = nat.load()
-    prev = lib.cc3d_gpu_set_tile_pass(nat.TILE_PASSES[name])
+    if name == "model":
+        from . import costmodel
+        try:
+            costmodel.get_params()
+        except ValueError:
+            costmodel.load()
+    prev = nat.load().cc3d_gpu_set_tile_pass(config_code(name))
     if prev < 0:
         nat.check(prev)
-    return {v: k for k, v in nat.TILE_PASSES.items()}[prev]
+    return config_name(prev)
 
 
 def _volume(data: Any):
@@ -62,21 +92,22 @@ def _volume(data: Any):
 
 
 def tile_pass_choice(data: Any, connectivity: int = 26, binary_image: bool = False) -> str:
-    """The variant a labelling of `data` would use now."""
+    """The configuration a labelling of `data` would use now."""
     ptr, code, sx, sy, sz, mem, stream, keep = _volume(data)
-    v = nat.load().cc3d_gpu_tile_pass_choice(code, sx, sy, sz, int(connectivity), int(bool(binary_image)))
-    return VARIANTS[v - 1]
+    return config_name(nat.load().cc3d_gpu_tile_pass_choice(code, sx, sy, sz, int(connectivity),
+                                                           int(bool(binary_image))))
 
 
 def autotune(data: Any, connectivity: int = 26, binary_image: bool = False, repeats: int = 2) -> Dict[str, Any]:
-    """Time every tile-pass variant on `data` and record the faster one for its
-    class.  Returns {"best": name, "ms": {name: milliseconds}}."""
+    """Time every tile-pass configuration on `data` and record the fastest for
+    its class.  Returns {"best": name, "ms": {name: milliseconds}}."""
     ptr, code, sx, sy, sz, mem, stream, keep = _volume(data)
     best = ctypes.c_int(0)
-    ms = (ctypes.c_double * 2)()
+    ms = (ctypes.c_double * len(CONFIGS))()
     nat.check(nat.load().cc3d_gpu_autotune(ptr, code, sx, sy, sz, int(connectivity), int(bool(binary_image)),
                                            mem, stream, int(repeats), ctypes.byref(best), ms))
-    return {"best": VARIANTS[best.value - 1], "ms": {VARIANTS[i]: ms[i] for i in range(2)}}
+    return {"best": config_name(best.value),
+            "ms": {CONFIGS[i]: ms[i] for i in range(len(CONFIGS)) if ms[i] >= 0}}
 
 
 def autotune_reset() -> None:

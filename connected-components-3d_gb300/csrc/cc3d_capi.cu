@@ -233,13 +233,22 @@ int size_bucket(int64_t voxels) {
 }
 
 int resolve_tile_pass(int dtype, int eff, int mode, int64_t voxels) {
-  if (g_tile_pass != CC3D_TILE_AUTO) return g_tile_pass;
+  if (g_tile_pass != CC3D_TILE_AUTO && g_tile_pass != CC3D_TILE_MODEL) return g_tile_pass;
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(dtype, eff, mode, size_bucket(voxels)));
   if (it != g_tuned.end()) return it->second;
   return CC3D_TILE_RUNS;
 }
 }  // namespace
+
+int cc3dgpu::tile_pass_for(int dtype, int eff_connectivity, int mode, int64_t voxels) {
+  return resolve_tile_pass(dtype, eff_connectivity, mode, voxels);
+}
+
+void cc3dgpu::record_tile_pass(int dtype, int eff_connectivity, int mode, int64_t voxels, int variant) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[std::make_tuple(dtype, eff_connectivity, mode, size_bucket(voxels))] = variant;
+}
 
 // error reporting shared with the other host translation units
 int cc3dgpu::api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
@@ -328,8 +337,16 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
 int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                            int64_t connectivity, int periodic_boundary, int binary_image,
                            int mem_flags, void* stream, cc3d_gpu_prepared* info) {
+  int code = CC3D_TILE_AUTO;
+  if (g_tile_pass == CC3D_TILE_MODEL && (mem_flags & CC3D_IN_DEVICE) && sx > 0 && sy > 0 && sz > 0 &&
+      g_model_loaded()) {
+    int choice = 0, confident = 0;
+    if (cc3d_gpu_cost_model_choose(in, dtype, sx, sy, sz, connectivity, binary_image, mem_flags, stream, 0.05f,
+                                   &choice, &confident) == CC3D_OK)
+      code = choice;
+  }
   return label_prepare(in, dtype, sx, sy, sz, connectivity, periodic_boundary, binary_image, mem_flags,
-                       stream, info, CC3D_TILE_AUTO);
+                       stream, info, code);
 }
 
 static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
@@ -371,7 +388,10 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
   const bool block8 = binary_image && conn == 8;
   const bool d3 = (eff == 26 || eff == 18 || eff == 6);
-  const int TY = d3 ? 8 : 64, TZ = d3 ? 8 : 1, HZ = d3 ? 1 : 0;
+  // tile-pass configuration: the caller's, the autotuned one for this class, or the default
+  if (variant == CC3D_TILE_AUTO) variant = resolve_tile_pass(dtype, eff, mode, voxels);
+  const TileCfg cfg = decode_tile_cfg(variant, d3);
+  const int TY = block8 ? 64 : cfg.ty, TZ = block8 ? 1 : cfg.tz, HZ = d3 ? 1 : 0;
 
   LabelArgs& a = job.args;
   memset(&a, 0, sizeof(a));
@@ -446,8 +466,7 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
     a.in = base + o_in;
     tm.mark(0);
   }
-  if (variant == CC3D_TILE_AUTO) variant = resolve_tile_pass(dtype, eff, mode, voxels);
-  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, variant, ntiles, s));
+  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, cfg.variant, ntiles, s));
   tm.mark(2);
   CK(launch_merge_edges(a, s));
   tm.mark(3);
@@ -697,11 +716,11 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   return CC3D_OK;
 }
 
-int cc3d_gpu_set_tile_pass(int variant) {
-  if (variant != CC3D_TILE_AUTO && variant != CC3D_TILE_RUNS && variant != CC3D_TILE_SCAN)
-    return fail(CC3D_ERR_INVALID, "unknown tile pass %d", variant);
+int cc3d_gpu_set_tile_pass(int code) {
+  if (!valid_tile_code(code) && code != CC3D_TILE_MODEL)
+    return fail(CC3D_ERR_INVALID, "unknown tile pass configuration %d", code);
   const int prev = g_tile_pass;
-  g_tile_pass = variant;
+  g_tile_pass = code;
   return prev;
 }
 
@@ -713,7 +732,9 @@ int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz, int
   if (sz == 1 && conn == 6) eff = 4;
   const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
   if (binary_image && conn == 8) return CC3D_TILE_RUNS;
-  return resolve_tile_pass(dtype, eff, mode, sx * sy * sz);
+  int code = resolve_tile_pass(dtype, eff, mode, sx * sy * sz);
+  if (!(eff == 26 || eff == 18 || eff == 6)) code &= 15;  // 2D: one tile shape
+  return code;
 }
 
 int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz, int64_t connectivity,
@@ -721,34 +742,49 @@ int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t
                       double* ms) {
   if (!best) return fail(CC3D_ERR_INVALID, "invalid arguments");
   if (repeats < 1) repeats = 1;
-  const int variants[2] = {CC3D_TILE_RUNS, CC3D_TILE_SCAN};
-  double t[2] = {0, 0};
-  for (int v = 0; v < 2; ++v) {
+  const int conn = (int)connectivity;
+  int eff = conn;
+  if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
+  if (sz == 1 && conn == 6) eff = 4;
+  const bool d3 = eff == 26 || eff == 18 || eff == 6;
+  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
+  const int ncfg = d3 ? CC3D_TILE_CONFIGS : 2;
+  double t[CC3D_TILE_CONFIGS];
+  int bi = 0;
+  for (int k = 0; k < CC3D_TILE_CONFIGS; ++k) t[k] = -1.0;
+  for (int k = 0; k < ncfg; ++k) {
+    const int code = cc3d_gpu_tile_config(k);
     double bestt = 1e300;
     for (int r = 0; r < repeats + 1; ++r) {  // the first run warms up
       cc3d_gpu_prepared info;
       const auto t0 = std::chrono::steady_clock::now();
       if (int rc = label_prepare(in, dtype, sx, sy, sz, connectivity, 0, binary_image, mem_flags, stream,
-                                 &info, variants[v]))
+                                 &info, code))
         return rc;
       const double dt = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       if (r > 0 && dt < bestt) bestt = dt;
     }
-    t[v] = bestt;
+    t[k] = bestt;
+    if (bestt < t[bi]) bi = k;
   }
-  const int conn = (int)connectivity;
-  int eff = conn;
-  if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
-  if (sz == 1 && conn == 6) eff = 4;
-  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
-  const int choice = t[1] < t[0] ? CC3D_TILE_SCAN : CC3D_TILE_RUNS;
+  const int choice = cc3d_gpu_tile_config(bi);
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tuned[std::make_tuple(dtype, eff, mode, size_bucket(sx * sy * sz))] = choice;
   }
   *best = choice;
-  if (ms) { ms[0] = t[0]; ms[1] = t[1]; }
+  if (ms)
+    for (int k = 0; k < CC3D_TILE_CONFIGS; ++k) ms[k] = t[k];
   return CC3D_OK;
+}
+
+int cc3d_gpu_tile_config(int index) {
+  static const int codes[CC3D_TILE_CONFIGS] = {
+      CC3D_TILE_RUNS | CC3D_TILE_8x8,  CC3D_TILE_SCAN | CC3D_TILE_8x8,
+      CC3D_TILE_RUNS | CC3D_TILE_4x16, CC3D_TILE_SCAN | CC3D_TILE_4x16,
+      CC3D_TILE_RUNS | CC3D_TILE_16x4, CC3D_TILE_SCAN | CC3D_TILE_16x4};
+  if (index < 0 || index >= CC3D_TILE_CONFIGS) return -1;
+  return codes[index];
 }
 
 void cc3d_gpu_autotune_reset(void) {

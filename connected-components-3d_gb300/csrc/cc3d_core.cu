@@ -185,6 +185,8 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
     uint32_t C = p.tinfo[tile].C;
     if (C > kTV) C = kTV;
     const uint32_t node0 = (uint32_t)(tile * kTV);
+    // a batch numbers each volume from 1: subtract the keys of the volumes before it
+    const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
     for (uint32_t c = lane; c < C; c += 32) {
       const uint32_t R = gfind(p.E, node0 + c, p.ctr);
       const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
       uint32_t lab = 0;
       if (w < p.nwords) {
         const uint32_t below = __ldg(p.bitmap + w) & ((1u << (key & 31)) - 1u);
-        lab = __ldg(p.prefix + w) + __popc(below) + 1u;
+        lab = __ldg(p.prefix + w) + __popc(below) + 1u - rank0;
       } else {
         atomicOr(&p.ctr->err, ERR_INDEX);
       }
@@ -206,7 +208,72 @@ template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
   k_resolve<<<152 * 16, 256, 0, s>>>(a);
   if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
   else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ batches
+// Per volume of a batch (one warp each): its estimate, provisional count,
+// first/last foreground rows from its tiles; its number of components from the
+// rank range of its bitmap words; the reference's output type for it
+// (cc3d/fastcc3d.pyx:429-434: uint16 below 65535 estimated labels, else
+// uint32; larger volumes are not batched).
+__global__ void __launch_bounds__(256) k_batch_finalize(LabelArgs p, int nvol, int64_t nwords,
+                                                         cc3dgpu::BatchResult* res) {
+  const int lane = threadIdx.x & 31;
+  const int v = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (v >= nvol) return;
+  VolGeo& g = p.vols[v];
+  const int64_t t0 = g.tile0;
+  const int64_t t1 = (v + 1 < nvol) ? p.vols[v + 1].tile0 : p.ntiles;
+  unsigned long long epl = 0, prov = 0;
+  long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+  for (int64_t t = t0 + lane; t < t1; t += 32) {
+    const TileInfo x = p.tinfo[t];
+    epl += x.epl;
+    prov += x.prov;
+    f = x.first_row < f ? x.first_row : f;
+    l = x.last_row > l ? x.last_row : l;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    epl += __shfl_down_sync(FULL, epl, o);
+    prov += __shfl_down_sync(FULL, prov, o);
+    f = min(f, (long long)__shfl_down_sync(FULL, f, o));
+    l = max(l, (long long)__shfl_down_sync(FULL, l, o));
+  }
+  if (lane == 0) {
+    const int64_t w1 = (v + 1 < nvol) ? p.vols[v + 1].word0 : nwords;
+    const unsigned long long r0 = g.word0 < nwords ? p.prefix[g.word0] : p.ctr->N;
+    const unsigned long long r1 = w1 < nwords ? p.prefix[w1] : p.ctr->N;
+    const unsigned long long voxels = (unsigned long long)(g.sx * g.sy * g.sz);
+    const unsigned long long max_labels = epl < voxels ? epl : voxels;
+    g.rank0 = r0;
+    g.out_code = max_labels < 65535ull ? 2 : 3;
+    res[v].N = r1 - r0;
+    res[v].epl = epl;
+    res[v].provisional = prov;
+    res[v].first_row = epl ? f : -1;
+    res[v].last_row = epl ? l : -1;
+    res[v].out_dtype = g.out_code;
+    res[v].status = 0;
+  }
+}
+
+cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, BatchResult* res,
+                                  cudaStream_t s) {
+  k_batch_finalize<<<(unsigned)((nvol + 7) / 8), 256, 0, s>>>(a, nvol, nwords, res);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  k_resolve<<<152 * 16, 256, 0, s>>>(a);
+  if (a.ty == 8 && a.tz == 8) k_write_batch<8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  else if (a.ty == 4 && a.tz == 16) k_write_batch<4, 16><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  else if (a.ty == 16 && a.tz == 4) k_write_batch<16, 4><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  else if (a.ty == 64 && a.tz == 1) k_write_batch<64, 1><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

@@ -181,7 +181,8 @@ cudaError_t launch_k1_scan(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   int use_tma = 0;
-  const bool aligned = ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
+  // (a batch of volumes of different shapes loads its rows without TMA)
+  const bool aligned = !a.vols && ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
                        a.sx < (1ll << 31) && a.sy < (1ll << 31) && a.sz < (1ll << 31);
   if (aligned && ntiles > 0) {
     using Encode = decltype(&cuTensorMapEncodeTiled);
@@ -218,23 +219,31 @@ cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, int variant, cudaStrea
   return cudaErrorInvalidValue;
 }
 
+// 3D tiles of 2048 voxels: 32 x TY x TZ with TY * TZ = 64
+template <typename T, int CONN, int MODE>
+cudaError_t launch_k1_3d(const LabelArgs& a, int64_t ntiles, int variant, cudaStream_t s) {
+  if (a.ty == 8 && a.tz == 8) return launch_k1<T, CONN, 8, 8, MODE>(a, ntiles, variant, s);
+  if (a.ty == 4 && a.tz == 16) return launch_k1<T, CONN, 4, 16, MODE>(a, ntiles, variant, s);
+  if (a.ty == 16 && a.tz == 4) return launch_k1<T, CONN, 16, 4, MODE>(a, ntiles, variant, s);
+  return cudaErrorInvalidValue;
+}
+
 template <typename T>
 cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool block8, int variant,
                                 int64_t ntiles, cudaStream_t s) {
   const bool d3 = conn == 26 || conn == 18 || conn == 6;
-  if (d3 && (a.ty != 8 || a.tz != 8)) return cudaErrorInvalidValue;
   if (!d3 && (a.ty != 64 || a.tz != 1)) return cudaErrorInvalidValue;
   const bool multi = mode == MODE_MULTI;
   switch (conn) {
     case 26:
-      return multi ? launch_k1<T, 26, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
-                   : launch_k1<T, 26, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
+      return multi ? launch_k1_3d<T, 26, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1_3d<T, 26, MODE_BINARY>(a, ntiles, variant, s);
     case 18:
-      return multi ? launch_k1<T, 18, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
-                   : launch_k1<T, 18, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
+      return multi ? launch_k1_3d<T, 18, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1_3d<T, 18, MODE_BINARY>(a, ntiles, variant, s);
     case 6:
-      return multi ? launch_k1<T, 6, 8, 8, MODE_MULTI>(a, ntiles, variant, s)
-                   : launch_k1<T, 6, 8, 8, MODE_BINARY>(a, ntiles, variant, s);
+      return multi ? launch_k1_3d<T, 6, MODE_MULTI>(a, ntiles, variant, s)
+                   : launch_k1_3d<T, 6, MODE_BINARY>(a, ntiles, variant, s);
     case 8:
       // binary 8-connected images are numbered by 2x2 blocks: block-parallel pass only
       if (block8) return launch_k1_runs<T, 8, 64, 1, MODE_BINARY, true>(a, ntiles, s);

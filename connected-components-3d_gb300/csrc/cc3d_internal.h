@@ -18,6 +18,27 @@ namespace cc3dgpu {
 constexpr int TILE_PASS_RUNS = 1;
 constexpr int TILE_PASS_SCAN = 2;
 
+// A tile-pass configuration (the CC3D_TILE_* codes of include/cc3d_gpu.h):
+// variant in bits 0-3, 3D tile shape in bits 4-7 (0: 32x8x8, 1: 32x4x16,
+// 2: 32x16x4).  2D images always use 32x64 tiles.
+struct TileCfg {
+  int variant;  // TILE_PASS_RUNS or TILE_PASS_SCAN
+  int ty, tz;
+};
+inline TileCfg decode_tile_cfg(int code, bool d3) {
+  TileCfg c;
+  c.variant = (code & 15) == TILE_PASS_SCAN ? TILE_PASS_SCAN : TILE_PASS_RUNS;
+  const int shape = (code >> 4) & 15;
+  if (!d3) { c.ty = 64; c.tz = 1; }
+  else if (shape == 1) { c.ty = 4; c.tz = 16; }
+  else if (shape == 2) { c.ty = 16; c.tz = 4; }
+  else { c.ty = 8; c.tz = 8; }
+  return c;
+}
+inline bool valid_tile_code(int code) {
+  return code == 0 || (((code & 15) == TILE_PASS_RUNS || (code & 15) == TILE_PASS_SCAN) && (code >> 4) <= 2);
+}
+
 #define CC3D_DECLARE_DTYPE_LAUNCHERS(SUF)                                              \
   cudaError_t launch_tile_local_##SUF(const LabelArgs& a, int conn, int mode,         \
                                       bool block8, int variant, int64_t ntiles,        \
@@ -42,10 +63,29 @@ CC3D_DECLARE_DTYPE_LAUNCHERS(f64)
 // fetched once through the runtime, so the library needs no -lcuda
 void* tensor_map_encoder();
 
+// whether a cost model has been trained or loaded (cc3d_costmodel.cu)
+bool g_model_loaded();
+
+// the tile pass CC3D_TILE_AUTO resolves to for a volume class (cc3d_capi.cu)
+int tile_pass_for(int dtype, int eff_connectivity, int mode, int64_t voxels);
+// record an autotuned choice for a volume class (cc3d_capi.cu)
+void record_tile_pass(int dtype, int eff_connectivity, int mode, int64_t voxels, int variant);
+
 // set the calling thread's error message (returns code); map a device error
 // word to a return code (cc3d_capi.cu)
 int api_fail(int code, const char* msg);
 int api_device_errors(unsigned err);
+
+// per-volume results of a batch (mirrors cc3d_gpu_volume_result)
+struct BatchResult {
+  uint64_t N;
+  uint64_t epl;
+  uint64_t provisional;
+  int64_t first_row;
+  int64_t last_row;
+  int32_t out_dtype;
+  int32_t status;
+};
 
 // dtype-independent stages (cc3d_core.cu)
 cudaError_t launch_merge_edges(const LabelArgs& a, cudaStream_t s);
@@ -54,6 +94,9 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* block_sums
 int64_t scan_blocks_needed(int64_t nwords);
 cudaError_t launch_write(const LabelArgs& a, void* out, int out_dtype, int64_t ntiles,
                          cudaStream_t s);
+cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, BatchResult* res,
+                                  cudaStream_t s);
+cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s);
 
 // statistics (cc3d_stats.cu)
 struct StatsArgs {

@@ -90,6 +90,21 @@ struct TileInfo {
   long long last_row;
 };
 
+// One volume of a batch.  A batch numbers the tiles of all its volumes one
+// after the other and lays their bitmap word ranges end to end, so that one
+// launch of each stage covers every volume: node ids and keys stay unique
+// across volumes, and a volume's labels are ranks within its word range.
+struct VolGeo {
+  const void* in;
+  void* out;
+  int64_t sx, sy, sz;
+  int ntx, nty, ntz;
+  int out_code;      // output element type (2 = uint16, 3 = uint32), set by k_batch_finalize
+  int64_t tile0;     // first tile of the volume in the batch
+  int64_t word0;     // first bitmap word of the volume
+  uint64_t rank0;    // number of keys before the volume's range (set by k_batch_finalize)
+};
+
 struct LabelArgs {
   const void* in;
   int64_t sx, sy, sz;
@@ -112,7 +127,38 @@ struct LabelArgs {
   Counters* ctr;
   int want_epl;
   int want_prov;
+  VolGeo* vols;                // batch descriptors (null for a single volume)
+  const uint32_t* tile_vol;    // [tiles] volume of every tile of a batch
 };
+
+// Geometry of the volume a tile belongs to, and the tile's place in it.
+struct TileGeo {
+  const void* in;
+  int64_t sx, sy, sz;
+  int ntx, nty;
+  int64_t wpr, key_row;  // bitmap words per row, key stride of a row
+  int64_t tile0;         // first tile of the volume (0 for a single volume)
+  int64_t word0;         // first bitmap word of the volume
+  int tx, ty, tz;        // tile coordinates inside the volume
+};
+
+__device__ __forceinline__ TileGeo tile_geo(const LabelArgs& p, int64_t tile) {
+  TileGeo g;
+  if (p.vols) {
+    const VolGeo& v = p.vols[p.tile_vol[tile]];
+    g.in = v.in; g.sx = v.sx; g.sy = v.sy; g.sz = v.sz; g.ntx = v.ntx; g.nty = v.nty;
+    g.wpr = v.ntx; g.key_row = (int64_t)v.ntx * 32; g.tile0 = v.tile0; g.word0 = v.word0;
+  } else {
+    g.in = p.in; g.sx = p.sx; g.sy = p.sy; g.sz = p.sz; g.ntx = p.ntx; g.nty = p.nty;
+    g.wpr = p.wpr; g.key_row = p.key_row; g.tile0 = 0; g.word0 = 0;
+  }
+  const int64_t local = tile - g.tile0;
+  g.tx = (int)(local % g.ntx);
+  const int64_t rest = local / g.ntx;
+  g.ty = (int)(rest % g.nty);
+  g.tz = (int)(rest / g.nty);
+  return g;
+}
 
 // ---------------------------------------------------------------- neighbours
 // Backward neighbour rows of a connectivity: (dy, dz) and which x offsets of
@@ -353,43 +399,75 @@ __global__ void k_wrap_pairs(LabelArgs p, int conn) {
 }
 
 // -------------------------------------------------------------- K3: write
+// one CTA expands one tile's run records into its volume's output
 template <typename OUT, int TY, int TZ>
-__global__ void __launch_bounds__(kThreads)
-k_write(LabelArgs p, OUT* out) {
+__device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT* out) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t tile = blockIdx.x;
-  const int tx = (int)(tile % p.ntx);
-  const int64_t rest = tile / p.ntx;
-  const int ty = (int)(rest % p.nty);
-  const int tz = (int)(rest / p.nty);
-  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)ty * TY, z0 = (int64_t)tz * TZ;
+  const TileGeo g = tile_geo(p, tile);
+  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   uint32_t C = p.tinfo[tile].C;
   if (C > kTV) {
     atomicOr(&p.ctr->err, ERR_INDEX);
     C = kTV;
   }
-  // final labels of the tile's components, resolved by k_resolve
+  // final labels of the tile's components, resolved by k_resolve.  Each warp
+  // owns 8 rows: the loads of all of them are issued before any store, so a
+  // warp waits for three rounds of loads (run masks and bases, run
+  // components, labels), not three per row.
+  constexpr int RPW = TY * TZ / (kThreads / 32);
+  static_assert(RPW * (kThreads / 32) == TY * TZ, "rows per warp");
   const uint32_t* lab = p.label + tile * kTV;
   const int64_t x = x0 + lane;
-  const bool xin = x < p.sx;
-  for (int ri = warp; ri < TY * TZ; ri += kThreads / 32) {
+  const bool xin = x < g.sx;
+  uint2 m[RPW];
+  int run[RPW];
+#pragma unroll
+  for (int j = 0; j < RPW; ++j) {
+    const int ri = warp + j * (kThreads / 32);
+    m[j] = __ldg(p.rmask + tile * kRowsPerTile + ri);
+    run[j] = (int)__ldg(p.rrow + tile * kRowsPerTile + ri);
+  }
+  uint32_t c[RPW];
+#pragma unroll
+  for (int j = 0; j < RPW; ++j) {
+    c[j] = 0xFFFFFFFFu;
+    if ((m[j].x >> lane) & 1u) {
+      const int k = __popc(m[j].y & lanemask_le(lane)) - 1;
+      const int r = run[j] + k;
+      c[j] = (k >= 0 && r < kTV) ? (uint32_t)__ldg(p.rcomp + tile * kTV + r) : 0xFFFFFFFEu;
+    }
+  }
+  OUT v[RPW];
+#pragma unroll
+  for (int j = 0; j < RPW; ++j) {
+    v[j] = OUT(0);
+    if (c[j] < C) v[j] = (OUT)__ldg(lab + c[j]);
+    else if (c[j] != 0xFFFFFFFFu) atomicOr(&p.ctr->err, ERR_INDEX);
+  }
+#pragma unroll
+  for (int j = 0; j < RPW; ++j) {
+    const int ri = warp + j * (kThreads / 32);
     const int ly = ri % TY, lz = ri / TY;
     const int64_t y = y0 + ly, z = z0 + lz;
-    if (y >= p.sy || z >= p.sz) continue;
-    const uint2 m = __ldg(p.rmask + tile * kRowsPerTile + ri);
-    OUT v = OUT(0);
-    if ((m.x >> lane) & 1u) {
-      const int k = __popc(m.y & lanemask_le(lane)) - 1;
-      const int run = (int)__ldg(p.rrow + tile * kRowsPerTile + ri) + k;
-      const uint16_t c = (k >= 0 && run < kTV) ? __ldg(p.rcomp + tile * kTV + run) : (uint16_t)0xFFFF;
-      if (c < C) {
-        v = (OUT)__ldg(lab + c);
-      } else {
-        atomicOr(&p.ctr->err, ERR_INDEX);
-      }
-    }
-    if (xin) out[(z * p.sy + y) * p.sx + x] = v;
+    if (xin && y < g.sy && z < g.sz) out[(z * g.sy + y) * g.sx + x] = v[j];
   }
+}
+
+template <typename OUT, int TY, int TZ>
+__global__ void __launch_bounds__(kThreads)
+k_write(LabelArgs p, OUT* out) {
+  write_tile<OUT, TY, TZ>(p, blockIdx.x, out);
+}
+
+// a batch: every volume has its own output buffer and element type
+template <int TY, int TZ>
+__global__ void __launch_bounds__(kThreads)
+k_write_batch(LabelArgs p) {
+  const int64_t tile = blockIdx.x;
+  const VolGeo& v = p.vols[p.tile_vol[tile]];
+  if (v.out_code == 2) write_tile<uint16_t, TY, TZ>(p, tile, static_cast<uint16_t*>(v.out));
+  else if (v.out_code == 3) write_tile<uint32_t, TY, TZ>(p, tile, static_cast<uint32_t*>(v.out));
+  else write_tile<uint64_t, TY, TZ>(p, tile, static_cast<uint64_t*>(v.out));
 }
 
 }  // namespace cc3dgpu

@@ -142,7 +142,10 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
   const bool block8 = binary_image && conn == 8;
   const bool d3 = (eff == 26 || eff == 18 || eff == 6);
-  const int TY = d3 ? 8 : 64, TZ = d3 ? 8 : 1, HZ = d3 ? 1 : 0;
+  // the variant follows the thread's choice; 3D tiles stay 32x8x8, the shape
+  // the scratch limit is stated for
+  const TileCfg cfg = decode_tile_cfg(cc3d_gpu_tile_pass_choice(dtype, sx, sy, sz, connectivity, binary_image) & 15, d3);
+  const int TY = block8 ? 64 : cfg.ty, TZ = block8 ? 1 : cfg.tz, HZ = d3 ? 1 : 0;
   LabelArgs a;
   memset(&a, 0, sizeof(a));
   a.sx = sx; a.sy = sy; a.sz = sz;
@@ -219,8 +222,7 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   h.last_row = -1;
   CKN(cudaMemcpyAsync(a.ctr, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   if (block8) CKN(cudaMemsetAsync(a.bitmap, 0, nwords * sizeof(uint32_t), s));
-  CKN(NOALLOC_DISPATCH(dtype, launch_tile_local, a, eff, mode, block8,
-                       cc3d_gpu_tile_pass_choice(dtype, sx, sy, sz, connectivity, binary_image), ntiles, s));
+  CKN(NOALLOC_DISPATCH(dtype, launch_tile_local, a, eff, mode, block8, cfg.variant, ntiles, s));
   CKN(launch_merge_edges(a, s));
   if (periodic_boundary) CKN(NOALLOC_DISPATCH(dtype, launch_wrap, a, eff, mode, s));
   CKN(launch_scan(a, nwords, bsum, nblocks, s));

@@ -137,11 +137,9 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   SMem& sm = reinterpret_cast<SMem*>(smem_raw + (mis ? 128u - mis : 0u))[warp];
   const int64_t tile = (int64_t)blockIdx.x * kScanWarps + warp;
   if (tile >= p.ntiles) return;  // the whole warp leaves
-  const int tx = (int)(tile % p.ntx);
-  const int64_t rest = tile / p.ntx;
-  const int ty = (int)(rest % p.nty);
-  const int tz = (int)(rest / p.nty);
-  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)ty * TY, z0 = (int64_t)tz * TZ;
+  const TileGeo g = tile_geo(p, tile);
+  const int tx = g.tx;
+  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   const uint32_t lt = (1u << lane) - 1u;
   unsigned err = 0;
 
@@ -183,13 +181,13 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         tma_load_3d(&sm.vals[slot][0], &tmap, &sm.bar[slot], (int)(x0 - G::PADX), cy, cz);
       }
     } else {
-      const T* in = static_cast<const T*>(p.in);
+      const T* in = static_cast<const T*>(g.in);
       for (int i = lane; i < CH * G::W; i += 32) {
         const int r = i / G::W, xi = i % G::W;
         const int64_t gx = x0 - G::PADX + xi, gy = cy + r, gz = cz;
         T v = T(0);
-        if (gx >= 0 && gx < p.sx && gy >= 0 && gy < p.sy && gz >= 0 && gz < p.sz)
-          v = in[(gz * p.sy + gy) * p.sx + gx];
+        if (gx >= 0 && gx < g.sx && gy >= 0 && gy < g.sy && gz >= 0 && gz < g.sz)
+          v = in[(gz * g.sy + gy) * g.sx + gx];
         sm.vals[slot][r * G::W + xi] = v;
       }
     }
@@ -446,7 +444,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
           const unsigned em = __ballot_sync(FULL, (v != prev) && (v != T(0)));
           if (em) {
             epl_acc += __popc(em);
-            const long long rg = (long long)((z0 - HZ + bz) * p.sy + gy);
+            const long long rg = (long long)((z0 - HZ + bz) * g.sy + gy);
             frow = rg < frow ? rg : frow;
             lrow = rg > lrow ? rg : lrow;
           }
@@ -510,15 +508,15 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       r = rootf(sm.runlab[run]);
       isnewc = !(sm.par[r] & kCompFlag);
     }
-    const uint32_t g = __match_any_sync(FULL, isnewc ? (uint32_t)r : 0x10000u + lane);
-    const bool leader = isnewc && lane == __ffs(g) - 1;
+    const uint32_t same = __match_any_sync(FULL, isnewc ? (uint32_t)r : 0x10000u + lane);
+    const bool leader = isnewc && lane == __ffs(same) - 1;
     const uint32_t NL = __ballot_sync(FULL, leader);
     const int ly = ri % TY, lz = ri / TY;
     const int64_t y = y0 + ly, z = z0 + lz;
     if (leader) {
       const uint32_t cid = C + __popc(NL & lt);
       sm.par[r] = (uint16_t)(kCompFlag | cid);
-      const uint32_t key = (uint32_t)((z * p.sy + y) * p.key_row + x0 + lane);
+      const uint32_t key = (uint32_t)(g.word0 * 32 + (z * g.sy + y) * g.key_row + x0 + lane);
       p.E[node0 + cid] = ((unsigned long long)key << 32) | (node0 + cid);
     }
     C += __popc(NL);
@@ -530,7 +528,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     if (lane == 0) {
       p.rmask[tile * kRowsPerTile + ri] = make_uint2(F, Sm);
       p.rrow[tile * kRowsPerTile + ri] = (uint16_t)base;
-      if (y < p.sy && z < p.sz) p.bitmap[(z * p.sy + y) * p.wpr + tx] = NL;
+      if (y < g.sy && z < g.sz) p.bitmap[g.word0 + (z * g.sy + y) * g.wpr + tx] = NL;
     }
   }
 
@@ -548,7 +546,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         const int rb = pos / 34, i = pos % 34;
         const int by = rb % BY, bz = rb / BY;
         const int64_t gx = x0 - 1 + i, gy = y0 - 1 + by, gz = z0 - HZ + bz;
-        const int64_t otile = (gx >> 5) + (int64_t)p.ntx * ((gy / TY) + (int64_t)p.nty * (gz / TZ));
+        const int64_t otile = g.tile0 + (gx >> 5) + (int64_t)g.ntx * ((gy / TY) + (int64_t)g.nty * (gz / TZ));
         const uint32_t local = (uint32_t)((gx & 31) + kTX * ((gy % TY) + TY * (gz % TZ)));
         e = make_uint2(node0 + (q & (kCompFlag - 1)), (uint32_t)(otile * kTV + local));
         has = true;

@@ -141,12 +141,10 @@ k_tile_runs(LabelArgs p) {
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t tile = blockIdx.x;
-  const int tx = (int)(tile % p.ntx);
-  const int64_t rest = tile / p.ntx;
-  const int ty = (int)(rest % p.nty);
-  const int tz = (int)(rest / p.nty);
-  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)ty * TY, z0 = (int64_t)tz * TZ;
-  const T* in = static_cast<const T*>(p.in);
+  const TileGeo g = tile_geo(p, tile);
+  const int tx = g.tx;
+  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
+  const T* in = static_cast<const T*>(g.in);
   const uint32_t lt = (1u << lane) - 1u;
 
   auto is_tile_row = [&](int rb) -> bool {
@@ -175,14 +173,14 @@ k_tile_runs(LabelArgs p) {
   for (int rb = warp; rb < NRB; rb += NW) {
     const int by = rb % BY, bz = rb / BY;
     const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
-    const bool rowin = (y >= 0) && (y < p.sy) && (z >= 0) && (z < p.sz);
+    const bool rowin = (y >= 0) && (y < g.sy) && (z >= 0) && (z < g.sz);
     const int64_t x = x0 + lane;
     T v = T(0), vl = T(0), vr = T(0);
     if (rowin) {
-      const T* rowp = in + (z * p.sy + y) * p.sx;
-      if (x < p.sx) v = rowp[x];
+      const T* rowp = in + (z * g.sy + y) * g.sx;
+      if (x < g.sx) v = rowp[x];
       if (lane == 0 && x0 > 0) vl = rowp[x0 - 1];
-      if (lane == 0 && x0 + kTX < p.sx) vr = rowp[x0 + kTX];
+      if (lane == 0 && x0 + kTX < g.sx) vr = rowp[x0 + kTX];
     }
     const S s = to_stored<S, T, MODE>(v);
     sv[rb * 32 + lane] = s;
@@ -197,7 +195,7 @@ k_tile_runs(LabelArgs p) {
       const unsigned m = __ballot_sync(FULL, (v != prev) && (v != T(0)));
       if (m) {
         epl_acc += __popc(m);
-        const long long rg = (long long)(y + p.sy * z);
+        const long long rg = (long long)(y + g.sy * z);
         frow = rg < frow ? rg : frow;
         lrow = rg > lrow ? rg : lrow;
       }
@@ -456,16 +454,16 @@ k_tile_runs(LabelArgs p) {
       const unsigned short r = par[ri * 32 + lane];
       const unsigned short c = cid[r];
       p.rcomp[tile * kTV + rbase[ri] + __popc(Sr & lt)] = c;
-      if (BLOCK8) atomicMin(&minblk[c], (uint32_t)((y >> 1) * p.key_row + ((x0 + lane) >> 1)));
+      if (BLOCK8) atomicMin(&minblk[c], (uint32_t)((y >> 1) * g.key_row + ((x0 + lane) >> 1)));
     }
     if (!BLOCK8) {
       const uint32_t rm = rootm[ri];
       if ((rm >> lane) & 1u) {
-        const uint32_t key = (uint32_t)((z * p.sy + y) * p.key_row + x0 + lane);
+        const uint32_t key = (uint32_t)(g.word0 * 32 + (z * g.sy + y) * g.key_row + x0 + lane);
         const uint32_t c = cid[ri * 32 + lane];
         p.E[node0 + c] = ((unsigned long long)key << 32) | (node0 + c);
       }
-      if (lane == 0 && y < p.sy && z < p.sz) p.bitmap[(z * p.sy + y) * p.wpr + tx] = rm;
+      if (lane == 0 && y < g.sy && z < g.sz) p.bitmap[g.word0 + (z * g.sy + y) * g.wpr + tx] = rm;
     }
   }
   if (BLOCK8) {
@@ -499,11 +497,11 @@ k_tile_runs(LabelArgs p) {
     if (!fg) return false;
     const unsigned short r = sfind_ro(par, (unsigned short)(kTV + h));
     if (r >= kTV) return false;
-    const unsigned short g = sfind_ro(parh, (unsigned short)h);
-    if (g != h && sfind_ro(par, (unsigned short)(kTV + g)) == r) return false;
+    const unsigned short grp = sfind_ro(parh, (unsigned short)h);
+    if (grp != h && sfind_ro(par, (unsigned short)(kTV + grp)) == r) return false;
     const int by = rb % BY, bz = rb / BY;
     const int64_t gy = y0 - 1 + by, gz = z0 - HZ + bz;
-    const int64_t otile = (gx >> 5) + (int64_t)p.ntx * ((gy / TY) + (int64_t)p.nty * (gz / TZ));
+    const int64_t otile = g.tile0 + (gx >> 5) + (int64_t)g.ntx * ((gy / TY) + (int64_t)g.nty * (gz / TZ));
     const uint32_t local = (uint32_t)(lx + kTX * ((gy % TY) + TY * (gz % TZ)));
     e = make_uint2(node0 + cid[r], (uint32_t)(otile * kTV + local));
     return true;

@@ -186,38 +186,140 @@ int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
 void cc3d_gpu_release_workspace(void);
 
 /*
- * Tile-pass variants and their autotuner.  No counterpart in the reference,
- * which has a single CPU algorithm per connectivity.  Every variant gives
- * identical labels; they differ only in speed:
- *   CC3D_TILE_RUNS  one 256-thread block per 32x8x8 (3D) / 32x64 (2D) tile:
- *                   rows cut into runs by ballots, unions of overlapping runs
- *                   in a shared-memory union-find.
- *   CC3D_TILE_SCAN  one warp per tile scanning its rows in raster order,
- *                   fed by TMA: runs copy the root of their backward
- *                   neighbours; unions only where two labels meet.
+ * Tile-pass configurations and their autotuner.  No counterpart in the
+ * reference, which has a single CPU algorithm per connectivity.  Every
+ * configuration gives identical labels; they differ only in speed.
+ * A configuration code is a variant ORed with a 3D tile shape:
+ *   CC3D_TILE_RUNS  one 256-thread block per tile: rows cut into runs by
+ *                   ballots, unions of overlapping runs in a shared-memory
+ *                   union-find.
+ *   CC3D_TILE_SCAN  one warp per tile scanning its rows in raster order, fed
+ *                   by TMA: runs copy the root of their backward neighbours;
+ *                   unions only where two labels meet.
+ *   CC3D_TILE_8x8 / _4x16 / _16x4   3D tiles of 32 x 8 x 8, 32 x 4 x 16 or
+ *                   32 x 16 x 4 voxels (x y z).  2D images always use 32 x 64.
  * Binary 8-connected images always use CC3D_TILE_RUNS (2x2-block numbering).
  *
- * cc3d_gpu_set_tile_pass: the calling thread's choice (CC3D_TILE_AUTO = the
- *   autotuned choice for the volume's class, else CC3D_TILE_RUNS); returns
- *   the previous setting.
- * cc3d_gpu_tile_pass_choice: the variant a labelling of this volume would use.
- * cc3d_gpu_autotune: times every variant on `in` (best of `repeats` after one
- *   warm-up run each), records the faster one for the volume's class (dtype,
- *   effective connectivity, binary or not, voxel count within a factor of 8)
- *   and returns it in *best, with the milliseconds of each variant in
- *   ms[0] (RUNS) and ms[1] (SCAN) when ms is not NULL.
+ * cc3d_gpu_set_tile_pass: the calling thread's configuration (CC3D_TILE_AUTO
+ *   = the autotuned choice for the volume's class, else RUNS | 8x8); returns
+ *   the previous setting, or CC3D_ERR_INVALID for an unknown code.
+ * cc3d_gpu_tile_pass_choice: the configuration a labelling of this volume
+ *   would use now.
+ * cc3d_gpu_tile_config: code of configuration `index` in 0..CC3D_TILE_CONFIGS-1
+ *   (RUNS|8x8, SCAN|8x8, RUNS|4x16, SCAN|4x16, RUNS|16x4, SCAN|16x4).
+ * cc3d_gpu_autotune: times every configuration on `in` (2D: the first two;
+ *   best of `repeats` after one warm-up run each), records the fastest for
+ *   the volume's class (dtype, effective connectivity, binary or not, voxel
+ *   count within a factor of 8) and returns it in *best; ms[index] gets each
+ *   configuration's milliseconds (-1 where not timed) when ms is not NULL
+ *   (room for CC3D_TILE_CONFIGS doubles).
  * cc3d_gpu_autotune_reset: forget every recorded choice.
  */
 #define CC3D_TILE_AUTO 0
 #define CC3D_TILE_RUNS 1
 #define CC3D_TILE_SCAN 2
-int cc3d_gpu_set_tile_pass(int variant);
+#define CC3D_TILE_8x8 0x00
+#define CC3D_TILE_4x16 0x10
+#define CC3D_TILE_16x4 0x20
+#define CC3D_TILE_CONFIGS 6
+#define CC3D_TILE_MODEL 3   /* policy: the cost model's choice per volume (below) */
+int cc3d_gpu_set_tile_pass(int code);
 int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz,
                               int64_t connectivity, int binary_image);
+int cc3d_gpu_tile_config(int index);
 int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                       int64_t connectivity, int binary_image, int mem_flags, void* stream,
                       int repeats, int* best, double* ms);
 void cc3d_gpu_autotune_reset(void);
+
+/*
+ * Learned cost model.  No counterpart in the reference.  A small FP32 MLP
+ * (CC3D_COST_FEATURES -> 64 -> 64 -> CC3D_TILE_CONFIGS, ReLU) predicts the
+ * natural log of the milliseconds every tile-pass configuration takes on a
+ * volume, from features sampled on the device; it is trained (mini-batch
+ * Adam, squared error over the measured outputs) on timings the autotuner
+ * produces.  Labels never depend on it.
+ *   cc3d_gpu_volume_features: the 16 features of a DEVICE volume: log2 of sx,
+ *     sy, sz and of the voxel count; element bytes / 8; connectivity / 26;
+ *     binary flag; and from 65,536 sampled voxels: foreground fraction,
+ *     log2(1 + distinct values among 4,096 samples) / 12, the fraction of
+ *     foreground samples equal to their +x, +y and +z neighbours, padding
+ *     waste of 32 in x and of 8 in y and z, and the fraction of foreground
+ *     samples that start a run in x.
+ *   cc3d_gpu_cost_model_train: X[n][16] features, Y[n][CONFIGS] log-ms (NaN
+ *     where not measured); replaces the process's model.
+ *   cc3d_gpu_cost_model_predict: Y[n][CONFIGS] predicted log-ms.
+ *   cc3d_gpu_cost_model_get / _set: the CC3D_COST_PARAMS floats of the model
+ *     (weights, then feature and output normalisation).
+ *   cc3d_gpu_cost_model_choose: the predicted fastest configuration for a
+ *     device volume; when the predicted runner-up is within `min_margin`
+ *     (relative, e.g. 0.05) the model is not confident and the exhaustive
+ *     autotuner decides instead (*confident = 0).
+ * With cc3d_gpu_set_tile_pass(CC3D_TILE_MODEL), labellings of device volumes
+ * use cc3d_gpu_cost_model_choose (margin 0.05) once a model is loaded;
+ * otherwise they behave as CC3D_TILE_AUTO.
+ */
+#define CC3D_COST_FEATURES 16
+#define CC3D_COST_PARAMS 5682
+int cc3d_gpu_volume_features(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                             int64_t connectivity, int binary_image, int mem_flags, void* stream,
+                             float* features);
+int cc3d_gpu_cost_model_train(const float* X, const float* Y, int n, int epochs, int batch, float lr,
+                              uint64_t seed, float* final_loss);
+int cc3d_gpu_cost_model_predict(const float* X, int n, float* Y);
+int cc3d_gpu_cost_model_get(float* params, int n);
+int cc3d_gpu_cost_model_set(const float* params, int n);
+int cc3d_gpu_cost_model_choose(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                               int64_t connectivity, int binary_image, int mem_flags, void* stream,
+                               float min_margin, int* choice, int* confident);
+
+/*
+ * Batches: many volumes labelled by one launch of each stage, the stage
+ * sequence captured once into a CUDA graph per batch layout (dtype,
+ * connectivity, tile-pass configuration and the list of shapes) and replayed
+ * while the layout repeats.  No counterpart in the reference, whose callers
+ * loop over cc3d.connected_components (the result of every volume is
+ * identical to that call's: labels, N, and the output type the Cython layer
+ * would choose, cc3d/fastcc3d.pyx:388-434).
+ *   - multilabel only (binary_image = 0, delta = 0), uint8/16/32 volumes of
+ *     one dtype, one connectivity; 2D connectivities need sz == 1;
+ *   - `in` and `out` are DEVICE buffers; `out` must hold voxels * 4 bytes and
+ *     receives uint16 or uint32 labels as results[i].out_dtype says;
+ *   - results[i] gets N, the estimate and first/last foreground row of
+ *     volume i; empty volumes get N = 0;
+ *   - the call returns when the labels are written.  With stream = NULL the
+ *     library waits for the legacy default stream, then runs on a stream of
+ *     its own (the legacy stream cannot be captured).
+ */
+typedef struct {
+  const void* in;
+  void* out;
+  int64_t sx, sy, sz;
+} cc3d_gpu_volume;
+
+typedef struct {
+  uint64_t N;
+  uint64_t epl;
+  uint64_t provisional;
+  int64_t first_row;
+  int64_t last_row;
+  int32_t out_dtype;   /* CC3D_U16 or CC3D_U32 */
+  int32_t status;      /* 0 */
+} cc3d_gpu_volume_result;
+
+int cc3d_gpu_label_batch(const cc3d_gpu_volume* volumes, int n, int dtype, int64_t connectivity,
+                         cc3d_gpu_volume_result* results, void* stream);
+/* Release this thread's batch workspace and graphs. */
+void cc3d_gpu_release_batch(void);
+/* Time every tile-pass configuration on this batch (2D: the first two; best
+   of `repeats` after the run that captures each graph), record the fastest
+   for the batch's class (dtype, connectivity, mean volume size within 8x) and
+   return it in *best; ms[index] gets each configuration's milliseconds (-1
+   where not timed) when ms is not NULL.  The labels of the last run are left
+   in the volumes' outputs and `results`. */
+int cc3d_gpu_autotune_batch(const cc3d_gpu_volume* volumes, int n, int dtype, int64_t connectivity,
+                            cc3d_gpu_volume_result* results, void* stream, int repeats, int* best,
+                            double* ms);
 
 /*
  * Labelling that allocates nothing.  No counterpart in the reference: the

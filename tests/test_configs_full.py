@@ -8,7 +8,7 @@
   and at 6 with periodic boundaries;
 * 8192^2 uint8 Bernoulli(0.5) at 8 and 4, binary and multilabel.
 
-Every case runs under both tile-pass variants; labels, N and dtypes must be
+Every case runs under every tile-pass configuration; labels, N and dtypes must be
 identical to the oracle's."""
 import numpy as np
 import pytest
@@ -18,7 +18,7 @@ import __graft_entry__ as entry
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ("runs", "scan")
+VARIANTS = ("runs/8x8", "scan/8x8", "runs/4x16", "scan/4x16", "runs/16x4", "scan/16x4")
 
 
 @pytest.fixture(scope="module")

@@ -11,10 +11,11 @@ import __graft_entry__ as entry
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module", params=["runs", "scan"])
+@pytest.fixture(scope="module", params=["runs/8x8", "scan/8x8", "runs/4x16", "scan/4x16", "runs/16x4",
+                                        "scan/16x4"])
 def cc3d(request):
-    """The package with one tile-pass variant selected: every parity test runs
-    once per variant."""
+    """The package with one tile-pass configuration selected: every parity
+    test runs once per configuration."""
     entry.build()
     import torch
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"

@@ -19,42 +19,56 @@ def cc3d():
 def test_choice_follows_the_thread_setting(cc3d):
     vol = np.zeros((40, 50, 60), np.uint32)
     assert cc3d.set_tile_pass("scan") == "auto"
-    assert cc3d.tile_pass_choice(vol) == "scan"
-    assert cc3d.set_tile_pass("runs") == "scan"
-    assert cc3d.tile_pass_choice(vol) == "runs"
+    assert cc3d.tile_pass_choice(vol) == "scan/8x8"
+    assert cc3d.set_tile_pass("runs/4x16") == "scan/8x8"
+    assert cc3d.tile_pass_choice(vol) == "runs/4x16"
+    cc3d.set_tile_pass("scan/16x4")
+    assert cc3d.tile_pass_choice(vol) == "scan/16x4"
+    # 2D images have one tile shape
+    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "scan/8x8"
     cc3d.set_tile_pass("auto")
     cc3d.autotune_reset()
-    assert cc3d.tile_pass_choice(vol) == "runs"  # the default without tuning data
+    assert cc3d.tile_pass_choice(vol) == "runs/8x8"  # the default without tuning data
     # binary 8-connected images always take the block pass (2x2-block numbering)
     cc3d.set_tile_pass("scan")
-    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs"
+    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs/8x8"
     cc3d.set_tile_pass("auto")
+    from cc3d_gb300.tuning import CONFIGS, config_code
+    lib = cc3d._native.load()
+    assert [lib.cc3d_gpu_tile_config(i) for i in range(len(CONFIGS))] == [config_code(c) for c in CONFIGS]
+    assert lib.cc3d_gpu_tile_config(len(CONFIGS)) == -1
 
 
 def test_unknown_variant_is_rejected(cc3d):
     lib = cc3d._native.load()
     assert lib.cc3d_gpu_set_tile_pass(7) == -1
+    assert lib.cc3d_gpu_set_tile_pass(0x31) == -1
     with pytest.raises(KeyError):
         cc3d.set_tile_pass("fastest")
 
 
 @pytest.mark.gpu
-def test_autotune_records_the_faster_variant(cc3d):
+def test_autotune_records_the_fastest_configuration(cc3d):
     import torch
     from cc3d_gb300 import synth
+    from cc3d_gb300.tuning import CONFIGS
     vol = synth.voronoi_volume((96, 128, 160), 200, 1 << 20, seed=21)
     cc3d.autotune_reset()
     for data in (vol, torch.from_numpy(vol).cuda()):
         res = cc3d.autotune(data, connectivity=26)
-        assert res["best"] in ("runs", "scan")
+        assert set(res["ms"]) == set(CONFIGS) and res["best"] in CONFIGS
         assert all(ms > 0 for ms in res["ms"].values())
         assert res["best"] == min(res["ms"], key=res["ms"].get)
         assert cc3d.tile_pass_choice(vol, connectivity=26) == res["best"]
         # the labels do not depend on the choice
         out, N = cc3d.connected_components(data, connectivity=26, return_N=True)
-        cc3d.set_tile_pass("runs" if res["best"] == "scan" else "scan")
-        out2, N2 = cc3d.connected_components(data, connectivity=26, return_N=True)
+        for other in CONFIGS:
+            cc3d.set_tile_pass(other)
+            out2, N2 = cc3d.connected_components(data, connectivity=26, return_N=True)
+            assert N == N2
+            assert np.array_equal(np.asarray(out.cpu() if hasattr(out, "cpu") else out),
+                                  np.asarray(out2.cpu() if hasattr(out2, "cpu") else out2))
         cc3d.set_tile_pass("auto")
-        assert N == N2
-        assert np.array_equal(np.asarray(out.cpu() if hasattr(out, "cpu") else out),
-                              np.asarray(out2.cpu() if hasattr(out2, "cpu") else out2))
+    img = synth.bernoulli_volume((300, 400), 0.5, seed=3)
+    res = cc3d.autotune(img, connectivity=4)
+    assert set(res["ms"]) == {"runs/8x8", "scan/8x8"}
