@@ -74,7 +74,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
@@ -83,9 +83,17 @@ class ClockSampler:
             for line in self.proc.stdout:
                 parts = [x.strip() for x in line.split(",")]
                 if len(parts) >= 9:
-                    self.samples.append(parts)
+                    self.samples.append((time.perf_counter(), parts))
         self.thread = threading.Thread(target=reader, daemon=True)
         self.thread.start()
+        # the timed region starts once samples are flowing
+        t0 = time.perf_counter()
+        while not self.samples and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def window(self, t0: float, t1: float):
+        """Summarise only the samples taken in [t0, t1] (the last earlier one if none)."""
+        self.span = (t0, t1)
 
     def stop(self):
         if self.proc is None:
@@ -97,17 +105,23 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        samples = list(self.samples)
+        if getattr(self, "span", None):
+            t0, t1 = self.span
+            inside = [x for x in samples if t0 <= x[0] <= t1]
+            samples = inside or [x for x in samples if x[0] <= t1][-1:]
+        rows = [r for _, r in samples]
+        sm = [float(s[1]) for s in rows if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in rows if s[2].replace(".", "").isdigit()]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
+        for s in rows:
             for name, v in zip(names, s[5:9]):
                 if v.strip().lower() in ("active", "1"):
                     reasons.add(name)
         return {"sm_mhz": pystats.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.samples)}
+                "reasons": sorted(reasons), "samples": len(rows)}
 
 
 def dist_setup():
@@ -194,6 +208,14 @@ def run_reference(args, world, rank):
     kind = "reference" if oracle.have_reference() else "port"
     vol = make_volume(0)
     cores = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+    # every process holds its copy of the input, the output and the union-find:
+    # take no more processes than host memory allows (about 3 x the volume each)
+    try:
+        with open("/proc/meminfo") as f:
+            avail = int(next(l for l in f if l.startswith("MemAvailable")).split()[1]) * 1024
+        cores = max(1, min(cores, int(avail * 0.6 // (3 * vol.nbytes))))
+    except (OSError, StopIteration, ValueError):
+        pass
     shm = "/dev/shm" if os.path.isdir("/dev/shm") else None
     with tempfile.TemporaryDirectory(dir=shm) as tmp:
         path = os.path.join(tmp, "volume.npy")
@@ -261,8 +283,10 @@ def run_gpu(args, world, rank, local):
         assert n == N
     ev1.record()
     torch.cuda.synchronize()
-    t_host = time.perf_counter() - t_host0
+    t_host1 = time.perf_counter()
+    t_host = t_host1 - t_host0
     barrier(world)
+    sampler.window(t_host0, t_host1)
     clocks = sampler.stop()
     stage = nat.profile_read()
     nat.profile_enable(False)
@@ -298,6 +322,7 @@ def run_gpu(args, world, rank, local):
         return n.value
 
     e2e_value = None
+    e2e_stages = None
     if not args.skip_e2e:
         for _ in range(args.warmup):
             e2e_step()
@@ -309,6 +334,12 @@ def run_gpu(args, world, rank, local):
         e2e_value = world * voxels * args.steps / t_e2e / 1e9
         expect = out.cpu().numpy().reshape(-1).view(np.uint8)
         assert np.array_equal(pin_out.numpy(), expect), "e2e labels differ from the device path"
+        # one more (untimed) step with the stage timer: where the end-to-end time goes
+        nat.profile_enable(True)
+        nat.profile_read()
+        e2e_step()
+        e2e_stages = {k: v[0] for k, v in nat.profile_read().items() if v[1]}
+        nat.profile_enable(False)
 
     # ---------------- roofline of the dominant kernel
     peak, peak_kind = load_peaks()
@@ -347,7 +378,9 @@ def run_gpu(args, world, rank, local):
                    "l2": "input (512 MiB) larger than L2, no flush"},
         "e2e": {"value": e2e_value, "unit": "GVoxels/s",
                 "h2d_bytes_per_step": voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
-                "path": "C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish), pinned host buffers"},
+                "path": "C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish), pinned host buffers; "
+                        "input and labels cross in 8 chunks overlapped with the tile pass and the writer",
+                "stage_ms": e2e_stages},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": kern_bytes[dom], "avg_launch_ms": dom_ms},
@@ -507,16 +540,15 @@ def run_costmodel(args):
     cm = cc3d.costmodel
     cc3d.build()
     t0 = time.perf_counter()
-    X, Y, _ = cm.collect(args.costmodel, seed=1)
+    X, Y, _ = cm.collect(args.costmodel, seed=1, repeats=2)
     t_collect = time.perf_counter() - t0
     loss = cm.train(X, Y, epochs=300, batch=256, lr=1e-3, seed=0)
     t_train = time.perf_counter() - t0 - t_collect
     n_test = max(50, args.costmodel // 5)
-    Xt, Yt, desc = cm.collect(n_test, seed=2)
+    Xt, Yt, desc = cm.collect(n_test, seed=2, repeats=2)
     P = cm.predict(Xt)
     reg = cm.regret(Yt, P)
-    srt = np.sort(np.where(np.isnan(Yt), np.inf, P), axis=1)
-    low_conf = float(np.mean(srt[:, 1] - srt[:, 0] < np.log1p(0.05)))
+    low_conf = reg["fallback_fraction"]
     if args.save_params:
         os.makedirs(os.path.dirname(os.path.abspath(args.save_params)), exist_ok=True)
         cm.save(args.save_params)

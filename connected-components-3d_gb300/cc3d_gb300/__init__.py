@@ -15,6 +15,8 @@ from . import _native  # noqa: F401
 from .tuning import autotune, autotune_reset, set_tile_pass, tile_pass_choice  # noqa: F401
 from .batch import autotune_batch, connected_components_batch  # noqa: F401
 from . import costmodel, tuning  # noqa: F401
+from .filters import dust, largest_k  # noqa: F401
+from .graphs import contacts, draw, each, region_graph, runs  # noqa: F401
 
 __all__ = [
     "build",
@@ -23,6 +25,13 @@ __all__ = [
     "statistics",
     "DimensionError",
     "connected_components_batch",
+    "dust",
+    "largest_k",
+    "contacts",
+    "region_graph",
+    "runs",
+    "draw",
+    "each",
     "autotune_batch",
     "autotune",
     "autotune_reset",

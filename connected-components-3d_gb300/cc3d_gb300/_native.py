@@ -52,6 +52,12 @@ EXPORTED = (
     "cc3d_gpu_cost_model_get",
     "cc3d_gpu_cost_model_set",
     "cc3d_gpu_cost_model_choose",
+    "cc3d_gpu_remap_labels",
+    "cc3d_gpu_zero_labels",
+    "cc3d_gpu_contacts",
+    "cc3d_gpu_contacts_copy",
+    "cc3d_gpu_run_starts",
+    "cc3d_gpu_run_starts_copy",
 )
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
 
@@ -127,6 +133,18 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_cost_model_set.argtypes = [vp, ci]
         lib.cc3d_gpu_cost_model_choose.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, ctypes.c_float,
                                                    ctypes.POINTER(ci), ctypes.POINTER(ci)]
+        lib.cc3d_gpu_remap_labels.argtypes = [vp, ci, i64, vp, ci, ctypes.c_uint64, vp, vp]
+        lib.cc3d_gpu_zero_labels.argtypes = [vp, ci, vp, ci, i64, vp, ctypes.c_uint64, vp]
+        lib.cc3d_gpu_remap_labels.restype = ci
+        lib.cc3d_gpu_contacts.argtypes = [vp, ci, i64, i64, i64, i64, u64p, vp]
+        lib.cc3d_gpu_contacts.restype = ci
+        lib.cc3d_gpu_contacts_copy.argtypes = [vp, vp, ctypes.c_uint64]
+        lib.cc3d_gpu_contacts_copy.restype = ci
+        lib.cc3d_gpu_run_starts.argtypes = [vp, ci, i64, u64p, vp]
+        lib.cc3d_gpu_run_starts.restype = ci
+        lib.cc3d_gpu_run_starts_copy.argtypes = [vp, vp, ctypes.c_uint64]
+        lib.cc3d_gpu_run_starts_copy.restype = ci
+        lib.cc3d_gpu_zero_labels.restype = ci
         for name in ("cc3d_gpu_volume_features", "cc3d_gpu_cost_model_train", "cc3d_gpu_cost_model_predict",
                      "cc3d_gpu_cost_model_get", "cc3d_gpu_cost_model_set", "cc3d_gpu_cost_model_choose"):
             getattr(lib, name).restype = ci

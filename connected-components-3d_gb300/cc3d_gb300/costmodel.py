@@ -205,17 +205,26 @@ def collect(n_volumes: int, seed: int, lo: int = 64, hi: int = 320,
     return np.stack(X), np.stack(Y), desc
 
 
-def regret(Y_true: np.ndarray, Y_pred: np.ndarray) -> Dict[str, float]:
+def regret(Y_true: np.ndarray, Y_pred: np.ndarray, min_margin: float = 0.05) -> Dict[str, float]:
     """How much slower the model's picks are than the measured best, over
-    volumes (Y in log-ms; NaN = not timed)."""
+    volumes (Y in log-ms; NaN = not timed).  "fallback" figures let the
+    exhaustive autotuner decide where the predicted runner-up is within
+    min_margin (as cc3d_gpu_cost_model_choose does)."""
     true = np.where(np.isnan(Y_true), np.inf, Y_true)
     pred = np.where(np.isnan(Y_true), np.inf, Y_pred)
     pick = pred.argmin(axis=1)
     best = true.min(axis=1)
     picked = true[np.arange(len(true)), pick]
     r = np.exp(picked - best) - 1.0
+    srt = np.sort(pred, axis=1)
+    unsure = (srt[:, 1] - srt[:, 0]) < np.log1p(min_margin)
+    picked_fb = np.where(unsure, best, picked)
+    r_fb = np.exp(picked_fb - best) - 1.0
     plain = true[:, 0]  # runs/8x8: the single default configuration
     return {"mean_regret": float(r.mean()), "p95_regret": float(np.percentile(r, 95)),
             "top1": float((pick == true.argmin(axis=1)).mean()),
             "time_vs_best": float(np.exp(picked).sum() / np.exp(best).sum()),
-            "time_vs_plain": float(np.exp(picked).sum() / np.exp(plain).sum())}
+            "time_vs_plain": float(np.exp(picked).sum() / np.exp(plain).sum()),
+            "fallback_fraction": float(unsure.mean()),
+            "fallback_mean_regret": float(r_fb.mean()),
+            "fallback_time_vs_plain": float(np.exp(picked_fb).sum() / np.exp(plain).sum())}

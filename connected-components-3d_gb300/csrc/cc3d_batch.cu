@@ -272,6 +272,8 @@ static int label_batch(const cc3d_gpu_volume* vols, int n, int dtype, int64_t co
     a.ty = TY;
     a.tz = TZ;
     a.ntiles = tiles;
+    a.tile_base = 0;
+    a.tile_end = tiles;
     a.nwords = words;
     a.edge_slots = edge_slots;
     a.want_epl = 1;

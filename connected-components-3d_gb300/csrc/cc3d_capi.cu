@@ -5,6 +5,7 @@
 // arguments like the reference's C++ entry points, stages host buffers, runs
 // the kernel pipeline on the caller's stream and maps device error words to
 // return codes.  No C++ exception crosses the ABI.
+#include <algorithm>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -72,8 +73,14 @@ struct Job {
   LabelArgs args;
 };
 
+// host <-> device copies of large volumes are cut into this many chunks of
+// whole tile layers (z), overlapped with the tile pass / the writer
+constexpr int kCopyChunks = 8;
+
 struct Workspace {
   cudaEvent_t ev[CC3D_PROFILE_STAGES + 1] = {};
+  cudaStream_t copy = nullptr;                 // second stream for chunked copies
+  cudaEvent_t chunk_ev[kCopyChunks + 1] = {};  // ordering between the two streams
   Job job;
   uint64_t next_token = 0;
   void* spill = nullptr;
@@ -107,7 +114,9 @@ int get_ws(Workspace*& out) {
     CK(cudaMallocHost((void**)&w.host_ctr, sizeof(Counters)));
     CK(cudaMallocHost((void**)&w.host_small, 64));
     CK(cudaStreamCreateWithFlags(&w.own, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&w.copy, cudaStreamNonBlocking));
     for (auto& e : w.ev) CK(cudaEventCreate(&e));
+    for (auto& e : w.chunk_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   out = &w;
   return CC3D_OK;
@@ -146,6 +155,22 @@ struct Carver {
     return at;
   }
 };
+
+// Tile layers [l0, l1) of chunk k out of n (whole z layers of tiles), and the
+// voxel range they cover; volumes with fewer than kCopyChunks tile layers, or
+// under 64 MiB, are one chunk.
+int copy_chunks(const LabelArgs& a, int64_t bytes) {
+  return (a.ntz >= kCopyChunks && bytes >= (64ll << 20)) ? kCopyChunks : 1;
+}
+void chunk_range(const LabelArgs& a, int k, int n, int64_t& t0, int64_t& t1, int64_t& v0, int64_t& v1) {
+  const int64_t l0 = (int64_t)a.ntz * k / n, l1 = (int64_t)a.ntz * (k + 1) / n;
+  const int64_t layer = (int64_t)a.ntx * a.nty;
+  t0 = l0 * layer;
+  t1 = l1 * layer;
+  const int64_t plane = a.sx * a.sy;
+  v0 = std::min<int64_t>(l0 * a.tz, a.sz) * plane;
+  v1 = std::min<int64_t>(l1 * a.tz, a.sz) * plane;
+}
 
 cudaStream_t pick_stream(Workspace& w, void* stream, int mem_flags) {
   if (stream) return (cudaStream_t)stream;
@@ -282,6 +307,11 @@ void cc3d_gpu_release_workspace(void) {
     if (kv.second.host_ctr) cudaFreeHost(kv.second.host_ctr);
     if (kv.second.host_small) cudaFreeHost(kv.second.host_small);
     if (kv.second.own) cudaStreamDestroy(kv.second.own);
+    if (kv.second.copy) cudaStreamDestroy(kv.second.copy);
+    for (auto& e : kv.second.chunk_ev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : kv.second.ev)
+      if (e) cudaEventDestroy(e);
     cudaSetDevice(prev);
   }
   g_ws.clear();
@@ -421,6 +451,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   // at most one edge per halo run head or halo column voxel
   a.edge_slots = (unsigned)((TY + 2) * (TZ + HZ) * 34 - kTV);
   a.ntiles = ntiles;
+  a.tile_base = 0;
+  a.tile_end = ntiles;
   a.want_epl = binary_image ? 0 : 1;
   a.want_prov = binary_image ? 1 : 0;
 
@@ -461,13 +493,41 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   if (block8) CK(cudaMemsetAsync(a.bitmap, 0, nwords * sizeof(uint32_t), s));
   StageTimer tm(*w, s);
   a.in = in;
-  if (stage_in) {
-    CK(cudaMemcpyAsync(base + o_in, in, voxels * isz, cudaMemcpyHostToDevice, s));
+  const int nchunks = stage_in ? copy_chunks(a, voxels * (int64_t)isz) : 1;
+  if (nchunks > 1) {
+    // the input arrives chunk by chunk on the copy stream; the tile pass of a
+    // chunk starts once it (and so every chunk before it, whose last plane is
+    // its halo) has landed
     a.in = base + o_in;
-    tm.mark(0);
+    CK(cudaEventRecord(w->chunk_ev[kCopyChunks], s));  // earlier work on this arena
+    CK(cudaStreamWaitEvent(w->copy, w->chunk_ev[kCopyChunks], 0));
+    for (int k = 0; k < nchunks; ++k) {
+      int64_t t0, t1, v0, v1;
+      chunk_range(a, k, nchunks, t0, t1, v0, v1);
+      CK(cudaMemcpyAsync(base + o_in + v0 * isz, (const char*)in + v0 * isz, (v1 - v0) * isz,
+                         cudaMemcpyHostToDevice, w->copy));
+      CK(cudaEventRecord(w->chunk_ev[k], w->copy));
+    }
+    for (int k = 0; k < nchunks; ++k) {
+      int64_t t0, t1, v0, v1;
+      chunk_range(a, k, nchunks, t0, t1, v0, v1);
+      CK(cudaStreamWaitEvent(s, w->chunk_ev[k], 0));
+      if (t1 == t0) continue;
+      LabelArgs ak = a;
+      ak.tile_base = t0;
+      ak.tile_end = t1;
+      CK(DISPATCH_DTYPE(dtype, launch_tile_local, ak, eff, mode, block8, cfg.variant, t1 - t0, s));
+    }
+    tm.mark(2);
+  } else {
+    if (stage_in) {
+      CK(cudaMemcpyAsync(base + o_in, in, voxels * isz, cudaMemcpyHostToDevice, s));
+      a.in = base + o_in;
+      tm.mark(0);
+    }
+    CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, cfg.variant, ntiles, s));
+    tm.mark(2);
   }
-  CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, cfg.variant, ntiles, s));
-  tm.mark(2);
   CK(launch_merge_edges(a, s));
   tm.mark(3);
   if (periodic_boundary) {
@@ -555,11 +615,35 @@ int cc3d_gpu_label_finish(uint64_t token, int64_t max_labels, void* out, int out
     }
   }
   StageTimer tm(*w, s);
-  CK(launch_write(job.args, dout, out_dtype, job.ntiles, s));
-  tm.mark(6);
-  if (stage_out) {
-    CK(cudaMemcpyAsync(out, dout, voxels * osz, cudaMemcpyDeviceToHost, s));
-    tm.mark(7);
+  const int nchunks = stage_out ? copy_chunks(job.args, voxels * (int64_t)osz) : 1;
+  if (nchunks > 1) {
+    // labels leave chunk by chunk on the copy stream while the writer
+    // produces the next chunk
+    CK(launch_resolve(job.args, s));
+    for (int k = 0; k < nchunks; ++k) {
+      int64_t t0, t1, v0, v1;
+      chunk_range(job.args, k, nchunks, t0, t1, v0, v1);
+      if (t1 > t0) {
+        LabelArgs ak = job.args;
+        ak.tile_base = t0;
+        ak.tile_end = t1;
+        CK(launch_write_tiles(ak, dout, out_dtype, t1 - t0, s));
+      }
+      CK(cudaEventRecord(w->chunk_ev[k], s));
+      CK(cudaStreamWaitEvent(w->copy, w->chunk_ev[k], 0));
+      CK(cudaMemcpyAsync((char*)out + v0 * osz, (const char*)dout + v0 * osz, (v1 - v0) * osz,
+                         cudaMemcpyDeviceToHost, w->copy));
+    }
+    CK(cudaEventRecord(w->chunk_ev[kCopyChunks], w->copy));
+    CK(cudaStreamWaitEvent(s, w->chunk_ev[kCopyChunks], 0));
+    tm.mark(6);
+  } else {
+    CK(launch_write(job.args, dout, out_dtype, job.ntiles, s));
+    tm.mark(6);
+    if (stage_out) {
+      CK(cudaMemcpyAsync(out, dout, voxels * osz, cudaMemcpyDeviceToHost, s));
+      tm.mark(7);
+    }
   }
   CK(cudaMemcpyAsync(w->host_ctr, job.args.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

@@ -278,6 +278,31 @@ cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t 
   return cudaGetLastError();
 }
 
+cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
+  k_resolve<<<152 * 16, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// the writer alone, for the tiles [a.tile_base, a.tile_base + count)
+template <typename OUT>
+cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s) {
+  if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_write_tiles(const LabelArgs& a, void* out, int out_dtype, int64_t count, cudaStream_t s) {
+  switch (out_dtype) {
+    case 2: return launch_write_tiles_t<uint16_t>(a, (uint16_t*)out, count, s);
+    case 3: return launch_write_tiles_t<uint32_t>(a, (uint32_t*)out, count, s);
+    case 4: return launch_write_tiles_t<uint64_t>(a, (uint64_t*)out, count, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_write(const LabelArgs& a, void* out, int out_dtype, int64_t ntiles, cudaStream_t s) {
   switch (out_dtype) {
     case 2: return launch_write_t<uint16_t>(a, (uint16_t*)out, ntiles, s);

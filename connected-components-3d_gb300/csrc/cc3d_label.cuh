@@ -129,6 +129,8 @@ struct LabelArgs {
   int want_prov;
   VolGeo* vols;                // batch descriptors (null for a single volume)
   const uint32_t* tile_vol;    // [tiles] volume of every tile of a batch
+  int64_t tile_base;           // first tile of this launch of the tile pass or the writer
+  int64_t tile_end;            // one past its last tile
 };
 
 // Geometry of the volume a tile belongs to, and the tile's place in it.
@@ -456,14 +458,14 @@ __device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT
 template <typename OUT, int TY, int TZ>
 __global__ void __launch_bounds__(kThreads)
 k_write(LabelArgs p, OUT* out) {
-  write_tile<OUT, TY, TZ>(p, blockIdx.x, out);
+  write_tile<OUT, TY, TZ>(p, p.tile_base + blockIdx.x, out);
 }
 
 // a batch: every volume has its own output buffer and element type
 template <int TY, int TZ>
 __global__ void __launch_bounds__(kThreads)
 k_write_batch(LabelArgs p) {
-  const int64_t tile = blockIdx.x;
+  const int64_t tile = p.tile_base + blockIdx.x;
   const VolGeo& v = p.vols[p.tile_vol[tile]];
   if (v.out_code == 2) write_tile<uint16_t, TY, TZ>(p, tile, static_cast<uint16_t*>(v.out));
   else if (v.out_code == 3) write_tile<uint32_t, TY, TZ>(p, tile, static_cast<uint32_t*>(v.out));

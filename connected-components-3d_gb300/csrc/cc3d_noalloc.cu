@@ -166,6 +166,8 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   a.nwords = nwords;
   a.edge_slots = (unsigned)((TY + 2) * (TZ + HZ) * 34 - kTV);
   a.ntiles = ntiles;
+  a.tile_base = 0;
+  a.tile_end = ntiles;
   a.want_epl = 0;
   a.want_prov = binary_image ? 1 : 0;
   const int64_t nblocks = scan_blocks_needed(nwords);

@@ -135,8 +135,8 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t mis = smem_addr(smem_raw) & 127u;
   SMem& sm = reinterpret_cast<SMem*>(smem_raw + (mis ? 128u - mis : 0u))[warp];
-  const int64_t tile = (int64_t)blockIdx.x * kScanWarps + warp;
-  if (tile >= p.ntiles) return;  // the whole warp leaves
+  const int64_t tile = p.tile_base + (int64_t)blockIdx.x * kScanWarps + warp;
+  if (tile >= p.tile_end) return;  // the whole warp leaves
   const TileGeo g = tile_geo(p, tile);
   const int tx = g.tx;
   const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;

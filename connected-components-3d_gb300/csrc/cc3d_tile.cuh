@@ -140,7 +140,7 @@ k_tile_runs(LabelArgs p) {
   __shared__ unsigned int edge_fill;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t tile = blockIdx.x;
+  const int64_t tile = p.tile_base + blockIdx.x;
   const TileGeo g = tile_geo(p, tile);
   const int tx = g.tx;
   const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;

@@ -186,6 +186,55 @@ int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
 void cc3d_gpu_release_workspace(void);
 
 /*
+ * Per-label rewrites of a labelled DEVICE volume: the element-wise halves of
+ * cc3d.dust (cc3d/__init__.py:71-155) and cc3d.largest_k
+ * (cc3d/__init__.py:199-279), whose per-label decisions the caller makes on
+ * the count table (cc3d_gpu_statistics).  Element types are given by their
+ * width in bytes (1, 2, 4, 8); labels are unsigned.  A label at or beyond
+ * table_len is an error (CC3D_ERR_INVALID).  Ordered on `stream`; return when
+ * done.
+ *   cc3d_gpu_remap_labels: out[i] = table[labels[i]] (largest_k's
+ *     renumbering, or a 0/1 mask for k = 1).
+ *   cc3d_gpu_zero_labels: image[i] = 0 where zero[labels[i]] != 0 (dust).
+ */
+int cc3d_gpu_remap_labels(const void* labels, int label_bytes, int64_t voxels, const void* table,
+                          int table_bytes, uint64_t table_len, void* out, void* stream);
+int cc3d_gpu_zero_labels(void* image, int image_bytes, const void* labels, int label_bytes,
+                         int64_t voxels, const uint8_t* zero, uint64_t table_len, void* stream);
+
+/*
+ * Region adjacency of a labelled DEVICE volume (x fastest; labels of
+ * label_bytes = 1, 2, 4 or 8, values below 2^32): the counting half of
+ * cc3d.contacts / cc3d.region_graph (cc3d/fastcc3d.pyx:1180-1256,
+ * cc3d/cc3d_graphs.hpp:238-466), with the reference's neighbourhood at the
+ * volume's faces.  cc3d_gpu_contacts counts, for every pair of touching
+ * nonzero labels (low, high), its contacts in four classes -- x face, y face,
+ * z face, edge or corner -- and returns the number of pairs;
+ * cc3d_gpu_contacts_copy then copies the pairs (low << 32 | high) and their
+ * four counts (uint32 [npairs][4]) to host memory.  The caller turns counts
+ * into areas (faces weigh wy*wz, wx*wz, wx*wy; 2D faces wy, wx; edges and
+ * corners 0; or 1 each for voxel counts).  Errors: 2D connectivities with
+ * sz != 1 (CC3D_ERR_RUNTIME, the reference's message), labels >= 2^32
+ * (CC3D_ERR_UNSUPPORTED).
+ */
+int cc3d_gpu_contacts(const void* labels, int label_bytes, int64_t sx, int64_t sy, int64_t sz,
+                      int64_t connectivity, uint64_t* npairs, void* stream);
+int cc3d_gpu_contacts_copy(uint64_t* pairs, uint32_t* counts, uint64_t npairs);
+
+/*
+ * Run starts of a labelled DEVICE array in memory order: the device half of
+ * cc3d.runs (cc3d/fastcc3d.pyx:1258-1277; extract_runs,
+ * cc3d/cc3d_graphs.hpp:470-502).  Position 0 and every position whose label
+ * differs from the previous element start a run; cc3d_gpu_run_starts returns
+ * their number and cc3d_gpu_run_starts_copy copies the positions (ascending)
+ * and the label at each to host memory.  Consecutive starts bound a run; the
+ * caller drops runs of label 0.
+ */
+int cc3d_gpu_run_starts(const void* labels, int label_bytes, int64_t voxels, uint64_t* nstarts,
+                        void* stream);
+int cc3d_gpu_run_starts_copy(uint64_t* positions, uint64_t* labels, uint64_t nstarts);
+
+/*
  * Tile-pass configurations and their autotuner.  No counterpart in the
  * reference, which has a single CPU algorithm per connectivity.  Every
  * configuration gives identical labels; they differ only in speed.

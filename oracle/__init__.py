@@ -350,3 +350,29 @@ def statistics(out_labels: np.ndarray, no_slice_conversion: bool = False) -> dic
             slices.append(None)
     output["bounding_boxes"] = slices
     return output
+
+
+def runs(labels: np.ndarray) -> dict:
+    """{label: [(start, end), ...]} in memory order, labels ascending: a
+    restatement of extract_runs (cc3d/cc3d_graphs.hpp:470-502) behind
+    cc3d.fastcc3d.runs (cc3d/fastcc3d.pyx:1258-1277).  A one-element input is
+    recorded whatever its label; an empty one raises like the reference."""
+    flat = _reshape_flat(np.asarray(labels))
+    if flat.dtype == np.bool_:
+        flat = flat.view(np.uint8)
+    if flat.dtype not in (np.uint8, np.uint16, np.uint32, np.uint64):
+        raise TypeError("Unsupported type: " + str(flat.dtype))
+    n = flat.size
+    if n == 0:
+        raise IndexError("Out of bounds on buffer access (axis 0)")
+    if n == 1:
+        return {int(flat[0]): [(0, 1)]}
+    starts = np.concatenate(([0], np.flatnonzero(flat[1:] != flat[:-1]) + 1))
+    ends = np.append(starts[1:], n)
+    out: dict = {}
+    for lab in np.unique(flat):
+        if lab == 0:
+            continue
+        sel = flat[starts] == lab
+        out[int(lab)] = list(zip(starts[sel].tolist(), ends[sel].tolist()))
+    return out

@@ -42,6 +42,9 @@ def _check(cc3d, vol, **kw):
         assert out.dtype == getattr(torch, exp.dtype.name), (v, kw)
         assert torch.equal(out, torch.from_numpy(exp).cuda()), (v, kw)
     cc3d.set_tile_pass("auto")
+    # host buffers: the input and the labels cross in chunks overlapped with the kernels
+    out, N = cc3d.connected_components(vol, return_N=True, **kw)
+    assert N == eN and out.dtype == exp.dtype and np.array_equal(out, exp), ("host", kw)
     return exp
 
 
