@@ -172,30 +172,35 @@ constexpr CUtensorMapDataType tma_type() {
                           : CU_TENSOR_MAP_DATA_TYPE_UINT64;
 }
 
-// The scan streams its box rows through TMA when the volume allows it: a
-// 16-byte aligned base and rows whose byte length is a multiple of 16 (the
-// copy engine's stride rule).  Otherwise the warps load the rows themselves.
+// A tensor map over the input for boxes of bw x bh x bd voxels, when the
+// volume allows TMA: a 16-byte aligned base and rows whose byte length is a
+// multiple of 16 (the copy engine's stride rule), one volume (a batch of
+// volumes has one base per volume).  Returns 1 if the map was made; with 0
+// the kernels load their boxes with plain loads.
+template <typename T>
+int encode_input_map(const LabelArgs& a, uint32_t bw, uint32_t bh, uint32_t bd, CUtensorMap* map) {
+  memset(map, 0, sizeof(*map));
+  const bool aligned = !a.vols && ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
+                       a.sx < (1ll << 31) && a.sy < (1ll << 31) && a.sz < (1ll << 31);
+  if (!aligned) return 0;
+  using Encode = decltype(&cuTensorMapEncodeTiled);
+  Encode enc = reinterpret_cast<Encode>(tensor_map_encoder());
+  if (!enc) return 0;
+  const cuuint64_t dims[3] = {(cuuint64_t)a.sx, (cuuint64_t)a.sy, (cuuint64_t)a.sz};
+  const cuuint64_t strides[2] = {(cuuint64_t)(a.sx * sizeof(T)), (cuuint64_t)(a.sx * a.sy * sizeof(T))};
+  const cuuint32_t box[3] = {bw, bh, bd};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  return enc(map, tma_type<T>(), 3, const_cast<void*>(a.in), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the raster scan: one warp per tile, box planes streamed through a TMA ring
 template <typename T, int CONN, int TY, int TZ, int MODE>
 cudaError_t launch_k1_scan(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   using G = ScanGeom<T, CONN, TY, TZ>;
   CUtensorMap map;
-  memset(&map, 0, sizeof(map));
-  int use_tma = 0;
-  // (a batch of volumes of different shapes loads its rows without TMA)
-  const bool aligned = !a.vols && ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
-                       a.sx < (1ll << 31) && a.sy < (1ll << 31) && a.sz < (1ll << 31);
-  if (aligned && ntiles > 0) {
-    using Encode = decltype(&cuTensorMapEncodeTiled);
-    if (Encode enc = reinterpret_cast<Encode>(tensor_map_encoder())) {
-      const cuuint64_t dims[3] = {(cuuint64_t)a.sx, (cuuint64_t)a.sy, (cuuint64_t)a.sz};
-      const cuuint64_t strides[2] = {(cuuint64_t)(a.sx * sizeof(T)), (cuuint64_t)(a.sx * a.sy * sizeof(T))};
-      const cuuint32_t box[3] = {(cuuint32_t)G::W, (cuuint32_t)G::CH, 1u};
-      const cuuint32_t estr[3] = {1u, 1u, 1u};
-      use_tma = enc(&map, tma_type<T>(), 3, const_cast<void*>(a.in), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-    }
-  }
+  const int use_tma = ntiles > 0 ? encode_input_map<T>(a, (uint32_t)G::W, (uint32_t)G::CH, 1u, &map) : 0;
   const size_t smem = scan_smem_bytes<T, CONN, TY, TZ>();
   cudaError_t e = cudaFuncSetAttribute(k_tile_scan<T, CONN, TY, TZ, MODE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -205,10 +210,15 @@ cudaError_t launch_k1_scan(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// the block-parallel pass: one CTA of 256 threads per tile
+// the block-parallel pass: one CTA of 256 threads per tile, its box staged by
+// one TMA copy
 template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
 cudaError_t launch_k1_runs(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  k_tile_runs<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
+  using B = TileBox<CONN, TY, TZ>;
+  CUtensorMap map;
+  const int use_tma =
+      ntiles > 0 ? encode_input_map<T>(a, (uint32_t)BoxRow<T>::W, (uint32_t)B::BY, (uint32_t)B::BZ, &map) : 0;
+  k_tile_runs<T, CONN, TY, TZ, MODE, BLOCK8><<<(unsigned)ntiles, kThreads, 0, s>>>(a, map, use_tma);
   return cudaGetLastError();
 }
 

@@ -28,52 +28,11 @@
 // edges that the rest of the pipeline (cc3d_label.cuh) consumes.
 #pragma once
 
-#include <cuda.h>
-
-#include "cc3d_label.cuh"
+#include "cc3d_tma.cuh"
 
 namespace cc3dgpu {
 
-// ------------------------------------------------------ TMA and mbarrier
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
-                                            int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_addr(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-      : "memory");
-}
-
 constexpr int kScanWarps = 2;           // tiles (warps) per CTA
-constexpr int kWaitLimit = 1 << 18;     // mbarrier polls before giving up
-constexpr unsigned ERR_WAIT = 128u;     // a chunk never arrived
 constexpr uint16_t kNoLabel = 0xFFFF;
 constexpr uint16_t kCompFlag = 0x8000;  // par[root] = flag | component id, final pass only
 

@@ -3,10 +3,15 @@
 // One CTA labels one 32 x TY x TZ tile (2048 voxels) with a one-voxel backward
 // halo, all in shared memory:
 //
-//   phase 0  rows of 32 values are loaded (one warp per row, 128 B coalesced
-//            for uint32) with the two halo columns; foreground and run-start
-//            masks come from warp ballots, and the provisional-label estimate
-//            (cc3d/cc3d.hpp:287-315) is counted on the tile's own rows.
+//   phase 0  the box (the tile, its halo rows and the two halo columns, padded
+//            in x to 16-byte boundaries) arrives by one TMA copy while the
+//            threads initialise the union-find; out-of-volume voxels are
+//            zero-filled by the copy engine, which is exactly the background
+//            the labelling needs at volume faces.  (Inputs whose rows are not
+//            16-byte multiples, and batches, load the box with plain loads.)
+//            Foreground and run-start masks come from warp ballots, and the
+//            provisional-label estimate (cc3d/cc3d.hpp:287-315) is counted on
+//            the tile's own rows.
 //   phase 2  every tile row is related to its backward rows.  Equalities at
 //            dx = 0 are one ballot per neighbour row; a union is queued only
 //            where a pair of overlapping runs starts.  Where the connectivity
@@ -18,14 +23,17 @@
 //            over the raster order.  Only the remaining voxels are queued as
 //            "items" that test their dx = +-1 neighbours and the halo columns.
 //            Unions and items go through small per-warp queues and are run in
-//            dense rounds (lane i takes entry i).  Halo rows are grouped with
-//            same-owner halo rows in a second forest.
+//            dense rounds (lane i takes entry i).
 //   phase 3  roots -> dense component ids in tile raster order, run-length
 //            records, component keys, the numbering bitmap, one edge per
-//            (component, halo group), the binary labellers' provisional count.
+//            halo run (or halo-column voxel) joined to a tile component --
+//            except where the same-owner voxel just before it (dx = 0, one row
+//            back in y, else in z) has the same value and joined the same
+//            component: both lie in one component of their own tile, so that
+//            edge would repeat -- and the binary labellers' provisional count.
 #pragma once
 
-#include "cc3d_label.cuh"
+#include "cc3d_tma.cuh"
 
 namespace cc3dgpu {
 
@@ -52,19 +60,30 @@ struct TileBox {
   }
 };
 
+
+// Staged box of one tile: box rows of W values, the tile's column x0 + x at
+// index PADX + x (x in [-1, 32]); the row starts 16-byte aligned in memory
+// and in the volume, as a TMA copy needs.
+template <typename T>
+struct BoxRow {
+  static constexpr int PADX = 16 / (int)sizeof(T);
+  static constexpr int W = 32 + 2 * PADX;
+};
+
 // One queued item of the tile pass: voxel x of box row rb, not covered by its
-// primary neighbour, tests its dx = +-1 neighbours and the halo columns.
-// Not inlined, so that its unions share one copy of the union-find code.
-// Returns a nonzero error code if a union ran out of budget.
-template <typename S, int CONN, int TY, int TZ, int MODE>
-__device__ __noinline__ int tile_item(int it, const S* sv, const S* scol0, const S* scol1,
-                                      const uint32_t* smask, unsigned short* par) {
+// primary neighbour, tests its dx = +-1 neighbours (the halo columns at the
+// tile's x faces).  Not inlined, so that its unions share one copy of the
+// union-find code.  Returns a nonzero error code if a union ran out of budget.
+template <typename T, typename S, int CONN, int TY, int TZ, int MODE>
+__device__ __noinline__ int tile_item(int it, const T* box, const uint32_t* smask, unsigned short* par) {
   using B = TileBox<CONN, TY, TZ>;
+  constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
   const int rb = it >> 5, x = it & 31;
-  const S s = sv[it];
+  auto sv = [&](int r, int xx) -> S { return to_stored<S, T, MODE>(box[r * W + PADX + xx]); };
+  const S s = sv(rb, x);
   const unsigned nR = B::node_of(rb, head_of(smask[rb], x));
   int err = 0;
-  if (x == 0 && rel<MODE>(s, scol0[rb])) {
+  if (x == 0 && rel<MODE>(s, sv(rb, -1))) {
     if (!sunite(par, (unsigned short)nR, (unsigned short)(B::CNODE + rb))) err = 1;
   }
 #pragma unroll 1
@@ -72,23 +91,13 @@ __device__ __noinline__ int tile_item(int it, const S* sv, const S* scol0, const
     int dy, dz, dxs;
     row_nb<CONN>(k, dy, dz, dxs);
     const int rbp = rb + dy + B::BY * dz;
-    unsigned target = 0xFFFFu;
-    if (dxs & 1) {
-      if (x == 0) {
-        if (rel<MODE>(s, scol0[rbp])) target = B::CNODE + rbp;
-      } else if (rel<MODE>(s, sv[rbp * 32 + x - 1])) {
-        target = B::node_of(rbp, head_of(smask[rbp], x - 1));
-      }
-      if (target != 0xFFFFu && !sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
+    if ((dxs & 1) && rel<MODE>(s, sv(rbp, x - 1))) {
+      const unsigned target = x == 0 ? B::CNODE + rbp : B::node_of(rbp, head_of(smask[rbp], x - 1));
+      if (!sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
     }
-    target = 0xFFFFu;
-    if (dxs & 4) {
-      if (x == 31) {
-        if (rel<MODE>(s, scol1[rbp])) target = B::CNODE + B::NRB + rbp;
-      } else if (rel<MODE>(s, sv[rbp * 32 + x + 1])) {
-        target = B::node_of(rbp, head_of(smask[rbp], x + 1));
-      }
-      if (target != 0xFFFFu && !sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
+    if ((dxs & 4) && rel<MODE>(s, sv(rbp, x + 1))) {
+      const unsigned target = x == 31 ? B::CNODE + B::NRB + rbp : B::node_of(rbp, head_of(smask[rbp], x + 1));
+      if (!sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
     }
   }
   return err;
@@ -96,7 +105,7 @@ __device__ __noinline__ int tile_item(int it, const S* sv, const S* scol0, const
 
 template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
 __global__ void __launch_bounds__(kThreads, 4)
-k_tile_runs(LabelArgs p) {
+k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
   using S = typename Stored<T, MODE>::type;
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
   constexpr int HZ = D3 ? 1 : 0;
@@ -108,6 +117,7 @@ k_tile_runs(LabelArgs p) {
   constexpr int NODES = CNODE + 2 * NRB;
   constexpr int NW = kThreads / 32;
   constexpr int NRN = RowNb<CONN>::n;
+  constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
   // neighbour rows (indices into row_nb) whose dx = 0 match makes a voxel's
   // other backward relations implied; -1 = none
   constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
@@ -118,12 +128,12 @@ k_tile_runs(LabelArgs p) {
   static_assert(NR == kRowsPerTile, "64 rows per tile");
   static_assert(NODES < 16384, "node ids must fit 14 bits");
   static_assert(!HAS_DX || MODE != MODE_BINARY4, "the binary 4-connected relation has no diagonals");
+  static_assert(W <= 256 && BY <= 256 && BZ <= 256, "TMA box dimensions");
 
-  __shared__ S sv[NRB * 32];
-  __shared__ S scol[2][NRB];
+  __shared__ __align__(128) T box[NRB * W];
+  __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t smask[NRB], fmask[NRB];
-  __shared__ unsigned short par[NODES];
-  __shared__ unsigned short parh[NODES - kTV];   // halo grouping forest (index - kTV)
+  __shared__ __align__(16) unsigned short par[NODES];
   // component ids (phase 3) share their storage with the phase-2 queues
   __shared__ __align__(16) unsigned short cid[kTV];
   __shared__ uint32_t rootm[NR];
@@ -144,7 +154,6 @@ k_tile_runs(LabelArgs p) {
   const TileGeo g = tile_geo(p, tile);
   const int tx = g.tx;
   const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
-  const T* in = static_cast<const T*>(g.in);
   const uint32_t lt = (1u << lane) - 1u;
 
   auto is_tile_row = [&](int rb) -> bool {
@@ -161,46 +170,80 @@ k_tile_runs(LabelArgs p) {
   auto node_of = [&](int rb, int h) -> unsigned {
     return is_tile_row(rb) ? (unsigned)(tile_row_of(rb) * 32 + h) : (unsigned)(HNODE + rb * 32 + h);
   };
+  // stored value of box row rb at tile column x (x in [-1, 32])
+  auto sv = [&](int rb, int x) -> S { return to_stored<S, T, MODE>(box[rb * W + PADX + x]); };
 
+  // ---- phase 0: the box arrives (TMA, or plain loads) while the forest is set up
   if (tid == 0) {
     local_err = 0;
     edge_fill = 0;
+    if (use_tma) {
+      mbar_init(&tbar, 1);
+      fence_mbar_init();
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&tbar, (uint32_t)(NRB * W * sizeof(T)));
+      tma_load_3d(box, &tmap, &tbar, (int)(x0 - PADX), (int)(y0 - 1), (int)(z0 - HZ));
+    }
   }
+  if (!use_tma) {
+    const T* in = static_cast<const T*>(g.in);
+    for (int rb = warp; rb < NRB; rb += NW) {
+      const int by = rb % BY, bz = rb / BY;
+      const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
+      const bool rowin = (y >= 0) && (y < g.sy) && (z >= 0) && (z < g.sz);
+      const int64_t x = x0 + lane;
+      T v = T(0), vl = T(0), vr = T(0);
+      if (rowin) {
+        const T* rowp = in + (z * g.sy + y) * g.sx;
+        if (x < g.sx) v = rowp[x];
+        if (lane == 0 && x0 > 0) vl = rowp[x0 - 1];
+        if (lane == 0 && x0 + kTX < g.sx) vr = rowp[x0 + kTX];
+      }
+      box[rb * W + PADX + lane] = v;
+      if (lane == 0) {
+        box[rb * W + PADX - 1] = vl;
+        box[rb * W + PADX + 32] = vr;
+      }
+    }
+  }
+  {
+    // identity forest, four nodes per store
+    uint2* p4 = reinterpret_cast<uint2*>(par);
+    for (int n = tid; n < NODES / 4; n += kThreads) {
+      const uint32_t b = 4u * n;
+      p4[n] = make_uint2(b | ((b + 1) << 16), (b + 2) | ((b + 3) << 16));
+    }
+    for (int n = (NODES / 4) * 4 + tid; n < NODES; n += kThreads) par[n] = (unsigned short)n;
+  }
+  if (use_tma) {
+    __syncthreads();  // the barrier is initialised before anyone polls it
+    if (!mbar_wait_bounded(&tbar, 0)) {
+      local_err = 3;
+      mbar_wait_bounded(&tbar, 0);  // let a late copy land before the CTA moves on
+    }
+  }
+  __syncthreads();
 
-  // ---- phase 0: stage rows and columns, runs, epl on the tile's own rows
+  // ---- masks of every box row, epl on the tile's own rows
   unsigned long long epl_acc = 0;
   long long frow = 0x7FFFFFFFFFFFFFFFLL, lrow = -1;
   for (int rb = warp; rb < NRB; rb += NW) {
     const int by = rb % BY, bz = rb / BY;
-    const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
-    const bool rowin = (y >= 0) && (y < g.sy) && (z >= 0) && (z < g.sz);
-    const int64_t x = x0 + lane;
-    T v = T(0), vl = T(0), vr = T(0);
-    if (rowin) {
-      const T* rowp = in + (z * g.sy + y) * g.sx;
-      if (x < g.sx) v = rowp[x];
-      if (lane == 0 && x0 > 0) vl = rowp[x0 - 1];
-      if (lane == 0 && x0 + kTX < g.sx) vr = rowp[x0 + kTX];
-    }
-    const S s = to_stored<S, T, MODE>(v);
-    sv[rb * 32 + lane] = s;
-    if (lane == 0) {
-      scol[0][rb] = to_stored<S, T, MODE>(vl);
-      scol[1][rb] = to_stored<S, T, MODE>(vr);
-    }
+    const T v = box[rb * W + PADX + lane];
     const bool trow = by >= 1 && by <= TY && bz >= HZ;
-    T prev = __shfl_up_sync(FULL, v, 1);
     if (p.want_epl && trow) {
-      if (lane == 0) prev = vl;
+      T prev = __shfl_up_sync(FULL, v, 1);
+      if (lane == 0) prev = box[rb * W + PADX - 1];
       const unsigned m = __ballot_sync(FULL, (v != prev) && (v != T(0)));
       if (m) {
         epl_acc += __popc(m);
-        const long long rg = (long long)(y + g.sy * z);
+        const long long rg = (long long)((y0 - 1 + by) + g.sy * (z0 - HZ + bz));
         frow = rg < frow ? rg : frow;
         lrow = rg > lrow ? rg : lrow;
       }
     }
     if (MODE != MODE_BINARY4) {
+      const S s = to_stored<S, T, MODE>(v);
       const S sl = (S)__shfl_up_sync(FULL, s, 1);
       const bool fg = is_fg(s);
       bool link = lane > 0 && fg && is_fg(sl);
@@ -213,9 +256,6 @@ k_tile_runs(LabelArgs p) {
       }
     }
   }
-  for (int n = tid; n < NODES; n += kThreads) par[n] = (unsigned short)n;
-  for (int n = tid; n < NODES - kTV; n += kThreads) parh[n] = (unsigned short)n;
-  __syncthreads();
 
   if (MODE == MODE_BINARY4) {
     // horizontal links of the reference's binary 4-connected labeller: the
@@ -223,7 +263,7 @@ k_tile_runs(LabelArgs p) {
     // both pixels have foreground directly above (they are joined through the
     // row above).  Halo rows keep single-voxel runs.
     for (int rb = warp; rb < NRB; rb += NW) {
-      const S s = sv[rb * 32 + lane];
+      const S s = sv(rb, lane);
       const S sl = (S)__shfl_up_sync(FULL, s, 1);
       const bool fg = is_fg(s);
       bool link = lane > 0 && fg && is_fg(sl);
@@ -233,7 +273,7 @@ k_tile_runs(LabelArgs p) {
       } else if (gy == 0) {
         link = link && (s == sl);
       } else {
-        const S a = sv[(rb - 1) * 32 + lane];
+        const S a = sv(rb - 1, lane);
         const S al = (S)__shfl_up_sync(FULL, a, 1);
         link = link && !(is_fg(a) && is_fg(al));
       }
@@ -244,13 +284,11 @@ k_tile_runs(LabelArgs p) {
         smask[rb] = F & ~L;
       }
     }
-    __syncthreads();
   }
+  __syncthreads();
 
   // ---- phase 2: unions through per-warp queues
   int uqn = 0, iqn = 0;  // warp-uniform queue fills
-  unsigned short* P = par;
-  int lim = NODES;
 
   auto flush_unions = [&](int upto) {
     // run entries [upto, uqn) in dense rounds of 32
@@ -260,8 +298,8 @@ k_tile_runs(LabelArgs p) {
       if (lane < n) {
         const uint32_t e = uq[warp][uqn - n + lane];
         const int a = (int)(e >> 16), b = (int)(e & 0xFFFFu);
-        if (a >= lim || b >= lim) local_err = 2;
-        else if (!sunite(P, (unsigned short)a, (unsigned short)b)) local_err = 1;
+        if (a >= NODES || b >= NODES) local_err = 2;
+        else if (!sunite(par, (unsigned short)a, (unsigned short)b)) local_err = 1;
       }
       uqn -= n;
       __syncwarp();
@@ -281,8 +319,7 @@ k_tile_runs(LabelArgs p) {
     while (iqn > upto) {
       const int n = iqn - upto < 32 ? iqn - upto : 32;
       if (lane < n) {
-        if (tile_item<S, CONN, TY, TZ, MODE>(iq[warp][iqn - n + lane], sv, scol[0], scol[1], smask, par))
-          local_err = 1;
+        if (tile_item<T, S, CONN, TY, TZ, MODE>(iq[warp][iqn - n + lane], box, smask, par)) local_err = 1;
       }
       iqn -= n;
       __syncwarp();
@@ -292,7 +329,7 @@ k_tile_runs(LabelArgs p) {
   // tile rows
   for (int ri = warp; ri < NR; ri += NW) {
     const int rb = box_row_of(ri);
-    const S s = sv[rb * 32 + lane];
+    const S s = sv(rb, lane);
     const uint32_t F = fmask[rb], Sr = smask[rb];
     const bool fg = (F >> lane) & 1u;
     const unsigned nR = (unsigned)(ri * 32 + head_of(Sr, lane));
@@ -302,7 +339,7 @@ k_tile_runs(LabelArgs p) {
       int dy, dz, dxs;
       row_nb<CONN>(k, dy, dz, dxs);
       const int rbp = rb + dy + BY * dz;
-      const S w = sv[rbp * 32 + lane];
+      const S w = sv(rbp, lane);
       Sp[k] = smask[rbp];
       M0[k] = __ballot_sync(FULL, fg && rel<MODE>(s, w));
     }
@@ -330,68 +367,18 @@ k_tile_runs(LabelArgs p) {
     } else if (F & 1u) {
       // same-row neighbour across the x seam
       const S s0 = (S)__shfl_sync(FULL, s, 0);
-      const S c0 = scol[0][rb];
+      const S c0 = sv(rb, -1);
       bool r0;
       if (MODE == MODE_MULTI) r0 = (s0 == c0);
       else if (MODE == MODE_BINARY4) {
         const int64_t gy = y0 - 1 + rb % BY;
-        r0 = is_fg(c0) && (gy == 0 ? (s0 == c0)
-                                   : !(is_fg(sv[(rb - 1) * 32]) && is_fg(scol[0][rb - 1])));
+        r0 = is_fg(c0) && (gy == 0 ? (s0 == c0) : !(is_fg(sv(rb - 1, 0)) && is_fg(sv(rb - 1, -1))));
       } else r0 = is_fg(c0);
       if (r0) push_unions(1u, (unsigned)(ri * 32), (unsigned)(CNODE + rb));
     }
   }
   flush_items(0);
   flush_unions(0);
-
-  // halo rows: group with backward halo rows of the same owner (dx = 0 only;
-  // an incomplete grouping only costs extra edges)
-  P = parh;
-  lim = NODES - kTV;
-  if (MODE != MODE_BINARY4) {
-    for (int rb = warp; rb < NRB; rb += NW) {
-      if (is_tile_row(rb)) continue;
-      const S s = sv[rb * 32 + lane];
-      const uint32_t F = fmask[rb], Sr = smask[rb];
-      const bool fg = (F >> lane) & 1u;
-      const int own = row_owner(rb);
-      const unsigned nR = (unsigned)(rb * 32 + head_of(Sr, lane));
-#pragma unroll
-      for (int k = 0; k < NRN; ++k) {
-        int dy, dz, dxs;
-        row_nb<CONN>(k, dy, dz, dxs);
-        const int by = rb % BY + dy, bz = rb / BY + dz;
-        if (by < 0 || by >= BY || bz < 0 || bz >= BZ) continue;
-        const int rbp = rb + dy + BY * dz;
-        if (is_tile_row(rbp) || row_owner(rbp) != own) continue;
-        const S w = sv[rbp * 32 + lane];
-        const uint32_t Spk = smask[rbp];
-        const uint32_t M = __ballot_sync(FULL, fg && rel<MODE>(s, w));
-        push_unions(M & (Sr | Spk | ~(M << 1)), nR, (unsigned)(rbp * 32 + head_of(Spk, lane)));
-      }
-    }
-    flush_unions(0);
-    // halo columns: group with backward voxels of the same column and owner
-    for (int c = tid; c < 2 * NRB; c += kThreads) {
-      const int side = c / NRB, rb = c % NRB;
-      const S s = scol[side][rb];
-      if (!is_fg(s)) continue;
-      const int own = row_owner(rb);
-#pragma unroll
-      for (int k = 0; k < NRN; ++k) {
-        int dy, dz, dxs;
-        row_nb<CONN>(k, dy, dz, dxs);
-        if (!(dxs & 2)) continue;
-        const int by = rb % BY + dy, bz = rb / BY + dz;
-        if (by < 0 || by >= BY || bz < 0 || bz >= BZ) continue;
-        const int rbp = rb + dy + BY * dz;
-        if (row_owner(rbp) != own) continue;
-        if (rel<MODE>(s, scol[side][rbp]))
-          if (!sunite(parh, (unsigned short)(CNODE - kTV + c), (unsigned short)(CNODE - kTV + side * NRB + rbp)))
-            local_err = 1;
-      }
-    }
-  }
   __syncthreads();
 
   // ---- phase 3a: component roots per tile row, run counts per row
@@ -475,30 +462,49 @@ k_tile_runs(LabelArgs p) {
     }
   }
 
-  // ---- phase 3c: one edge per (tile component, halo group) into the tile's
-  // own edge slots
+  // ---- phase 3c: one edge per halo run / halo-column voxel joined to a tile
+  // component, into the tile's own edge slots
+  // the same-owner box row just before rb (one back in y, else in z), or -1
+  auto prev_row = [&](int rb) -> int {
+    const int by = rb % BY, bz = rb / BY, own = row_owner(rb);
+    if (by > 0 && row_owner(rb - 1) == own) return rb - 1;
+    if (bz > 0 && row_owner(rb - BY) == own) return rb - BY;
+    return -1;
+  };
   auto halo_edge = [&](int h, uint2& e) -> bool {
-    int rb, lx;
+    int rb, lx, xi;  // xi: the voxel's tile column (-1 and 32 for the halo columns)
     int64_t gx;
-    bool fg;
+    unsigned short node;
     if (h < NRB * 32) {
       rb = h >> 5;
       lx = h & 31;
       if (is_tile_row(rb)) return false;
-      fg = ((smask[rb] >> lx) & 1u) != 0;  // run heads stand for their runs
+      if (!((smask[rb] >> lx) & 1u)) return false;  // run heads stand for their runs
+      xi = lx;
       gx = x0 + lx;
+      node = (unsigned short)(HNODE + h);
     } else {
       const int c = h - NRB * 32;
       rb = c % NRB;
-      fg = is_fg(scol[c / NRB][rb]);
-      gx = (c < NRB) ? x0 - 1 : x0 + kTX;
+      xi = (c < NRB) ? -1 : 32;
+      gx = x0 + xi;
       lx = (int)(gx & 31);
+      node = (unsigned short)(CNODE + c);
+      if (!is_fg(sv(rb, xi))) return false;
     }
-    if (!fg) return false;
-    const unsigned short r = sfind_ro(par, (unsigned short)(kTV + h));
+    const unsigned short r = sfind_ro(par, node);
     if (r >= kTV) return false;
-    const unsigned short grp = sfind_ro(parh, (unsigned short)h);
-    if (grp != h && sfind_ro(par, (unsigned short)(kTV + grp)) == r) return false;
+    const int rp = MODE == MODE_BINARY4 ? -1 : prev_row(rb);
+    if (rp >= 0) {
+      const S a = sv(rb, xi), b = sv(rp, xi);
+      if (is_fg(b) && (MODE == MODE_MULTI ? a == b : true)) {
+        unsigned short np;
+        if (xi < 0) np = (unsigned short)(CNODE + rp);
+        else if (xi > 31) np = (unsigned short)(CNODE + NRB + rp);
+        else np = (unsigned short)(HNODE + rp * 32 + head_of(smask[rp], xi));
+        if (sfind_ro(par, np) == r) return false;
+      }
+    }
     const int by = rb % BY, bz = rb / BY;
     const int64_t gy = y0 - 1 + by, gz = z0 - HZ + bz;
     const int64_t otile = g.tile0 + (gx >> 5) + (int64_t)g.ntx * ((gy / TY) + (int64_t)g.nty * (gz / TZ));
@@ -533,18 +539,19 @@ k_tile_runs(LabelArgs p) {
   // ---- provisional labels the reference's binary labeller would open
   unsigned int prov = 0;
   if (p.want_prov) {
+    auto colfg = [&](int rb, int xi) -> uint32_t { return is_fg(sv(rb, xi)) ? 1u : 0u; };
     if (BLOCK8) {
       // 2x2 blocks Y Z / X W; C D E F in the row above, B A to the left
       for (int q = tid; q < kTV / 4; q += kThreads) {
         const int b = q & 15, ri = 2 * (q >> 4);
         const int rb = box_row_of(ri);
         const uint32_t Fa = fmask[rb - 1], F0 = fmask[rb], F1 = fmask[rb + 1];
-        const uint32_t ca = is_fg(scol[0][rb - 1]) ? 1u : 0u, c0 = is_fg(scol[0][rb]) ? 1u : 0u;
-        const uint32_t c1 = is_fg(scol[0][rb + 1]) ? 1u : 0u, ra = is_fg(scol[1][rb - 1]) ? 1u : 0u;
+        const uint32_t ca = colfg(rb - 1, -1), c0 = colfg(rb, -1);
+        const uint32_t c1 = colfg(rb + 1, -1), ra = colfg(rb - 1, 32);
         const int x = 2 * b;
         const bool Y = (F0 >> x) & 1u, Z = (F0 >> (x + 1)) & 1u;
-        const bool X = (F1 >> x) & 1u, W = (F1 >> (x + 1)) & 1u;
-        if (!(Y || Z || X || W)) continue;
+        const bool X = (F1 >> x) & 1u, W_ = (F1 >> (x + 1)) & 1u;
+        if (!(Y || Z || X || W_)) continue;
         const bool Cc = x == 0 ? ca : (Fa >> (x - 1)) & 1u;
         const bool D = (Fa >> x) & 1u, Ee = (Fa >> (x + 1)) & 1u;
         const bool Fq = x + 2 == 32 ? ra : (Fa >> (x + 2)) & 1u;
@@ -557,15 +564,15 @@ k_tile_runs(LabelArgs p) {
       for (int ri = warp; ri < NR; ri += NW) {
         const int rb = box_row_of(ri);
         const uint32_t F = fmask[rb];
-        const S s = sv[rb * 32 + lane];
+        const S s = sv(rb, lane);
         uint32_t Lk;
         const int64_t gy = y0 + ri % TY, gz = z0 + ri / TY;
         if (MODE == MODE_BINARY4 && gy == 0 && gz == 0) {
           S sl = (S)__shfl_up_sync(FULL, s, 1);
-          if (lane == 0) sl = scol[0][rb];
+          if (lane == 0) sl = sv(rb, -1);
           Lk = __ballot_sync(FULL, is_fg(s) && s == sl);
         } else {
-          Lk = (F << 1) | (is_fg(scol[0][rb]) ? 1u : 0u);
+          Lk = (F << 1) | colfg(rb, -1);
         }
 #pragma unroll
         for (int k = 0; k < NRN; ++k) {
@@ -574,8 +581,8 @@ k_tile_runs(LabelArgs p) {
           const int rbp = rb + dy + BY * dz;
           const uint32_t Fp = fmask[rbp];
           if (dxs & 2) Lk |= Fp;
-          if (dxs & 1) Lk |= (Fp << 1) | (is_fg(scol[0][rbp]) ? 1u : 0u);
-          if (dxs & 4) Lk |= (Fp >> 1) | (is_fg(scol[1][rbp]) ? 0x80000000u : 0u);
+          if (dxs & 1) Lk |= (Fp << 1) | colfg(rbp, -1);
+          if (dxs & 4) Lk |= (Fp >> 1) | (colfg(rbp, 32) << 31);
         }
         if (lane == 0) prov += __popc(F & ~Lk);
       }
@@ -612,7 +619,8 @@ k_tile_runs(LabelArgs p) {
     ti.last_row = l;
     p.tinfo[tile] = ti;
     if (nedges > p.edge_slots) atomicOr(&p.ctr->err, ERR_EDGE_OVERFLOW);
-    if (local_err) atomicOr(&p.ctr->err, local_err == 2 ? ERR_INDEX : ERR_LOCAL_BUDGET);
+    if (local_err)
+      atomicOr(&p.ctr->err, local_err == 3 ? ERR_WAIT : (local_err == 2 ? ERR_INDEX : ERR_LOCAL_BUDGET));
   }
 }
 
