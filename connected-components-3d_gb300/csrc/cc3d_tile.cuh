@@ -20,10 +20,12 @@
 //            needs nothing else: each of its other backward neighbours that it
 //            relates to is also a neighbour of the primary one, related to it,
 //            and earlier in raster order, so that pair is joined by induction
-//            over the raster order.  Only the remaining voxels are queued as
-//            "items" that test their dx = +-1 neighbours and the halo columns.
-//            Unions and items go through small per-warp queues and are run in
-//            dense rounds (lane i takes entry i).
+//            over the raster order.  Only the remaining voxels test their
+//            dx = +-1 neighbours (the halo columns at the x faces), again as
+//            ballots, and a union is queued only for a pair of runs that
+//            neither the voxel before it nor the dx = 0 relation already
+//            joins.  Unions go through small per-warp queues and are run in
+//            dense rounds (lane i takes entry i), every lane at one call site.
 //   phase 3  roots -> dense component ids in tile raster order, run-length
 //            records, component keys, the numbering bitmap, one edge per
 //            halo run (or halo-column voxel) joined to a tile component --
@@ -70,36 +72,24 @@ struct BoxRow {
   static constexpr int W = 32 + 2 * PADX;
 };
 
-// One queued item of the tile pass: voxel x of box row rb, not covered by its
-// primary neighbour, tests its dx = +-1 neighbours (the halo columns at the
-// tile's x faces).  Not inlined, so that its unions share one copy of the
-// union-find code.  Returns a nonzero error code if a union ran out of budget.
-template <typename T, typename S, int CONN, int TY, int TZ, int MODE>
-__device__ __noinline__ int tile_item(int it, const T* box, const uint32_t* smask, unsigned short* par) {
-  using B = TileBox<CONN, TY, TZ>;
-  constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
-  const int rb = it >> 5, x = it & 31;
-  auto sv = [&](int r, int xx) -> S { return to_stored<S, T, MODE>(box[r * W + PADX + xx]); };
-  const S s = sv(rb, x);
-  const unsigned nR = B::node_of(rb, head_of(smask[rb], x));
+// Runs the queued unions q[from, to) of one warp, lane i taking entry from + i
+// of each round of 32.  Entries are (a << 16) | b.  Not inlined, so that every
+// queue site shares one copy of the union-find code.  Returns 2 for a node id
+// out of range, 1 if a union ran out of budget, else 0.
+static __device__ __noinline__ int run_unions(const uint32_t* q, int from, int to, unsigned short* par, int nodes,
+                                       int lane) {
+  __syncwarp();
   int err = 0;
-  if (x == 0 && rel<MODE>(s, sv(rb, -1))) {
-    if (!sunite(par, (unsigned short)nR, (unsigned short)(B::CNODE + rb))) err = 1;
-  }
-#pragma unroll 1
-  for (int k = 0; k < RowNb<CONN>::n; ++k) {
-    int dy, dz, dxs;
-    row_nb<CONN>(k, dy, dz, dxs);
-    const int rbp = rb + dy + B::BY * dz;
-    if ((dxs & 1) && rel<MODE>(s, sv(rbp, x - 1))) {
-      const unsigned target = x == 0 ? B::CNODE + rbp : B::node_of(rbp, head_of(smask[rbp], x - 1));
-      if (!sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
-    }
-    if ((dxs & 4) && rel<MODE>(s, sv(rbp, x + 1))) {
-      const unsigned target = x == 31 ? B::CNODE + B::NRB + rbp : B::node_of(rbp, head_of(smask[rbp], x + 1));
-      if (!sunite(par, (unsigned short)nR, (unsigned short)target)) err = 1;
+  for (int r = from; r < to; r += 32) {
+    const int i = r + lane;
+    if (i < to) {
+      const uint32_t e = q[i];
+      const int a = (int)(e >> 16), b = (int)(e & 0xFFFFu);
+      if (a >= nodes || b >= nodes) err = 2;
+      else if (!sunite(par, (unsigned short)a, (unsigned short)b)) err = 1;
     }
   }
+  __syncwarp();
   return err;
 }
 
@@ -123,7 +113,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
   constexpr int PRI1 = (CONN == 18) ? 0 : -1;
   constexpr bool HAS_DX = (CONN == 26 || CONN == 18 || CONN == 8);
-  constexpr int QN = 64;                       // per-warp queue capacity
+  constexpr int QN = 128;                      // per-warp queue capacity
   static_assert(kTX * NR == kTV, "tile must hold 2048 voxels");
   static_assert(NR == kRowsPerTile, "64 rows per tile");
   static_assert(NODES < 16384, "node ids must fit 14 bits");
@@ -134,15 +124,14 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t smask[NRB], fmask[NRB];
   __shared__ __align__(16) unsigned short par[NODES];
-  // component ids (phase 3) share their storage with the phase-2 queues
+  // component ids (phase 3) share their storage with the phase-2 union queues
   __shared__ __align__(16) unsigned short cid[kTV];
   __shared__ uint32_t rootm[NR];
   __shared__ unsigned short rbase[NR + 1], cbase[NR + 1];
   __shared__ uint32_t minblk[BLOCK8 ? kTV : 1];
-  static_assert(NW * QN * (sizeof(uint32_t) + sizeof(unsigned short)) <= sizeof(unsigned short) * kTV,
+  static_assert(NW * QN * sizeof(uint32_t) <= sizeof(unsigned short) * kTV,
                 "queues must fit in the component-id storage");
-  uint32_t (*uq)[QN] = reinterpret_cast<uint32_t (*)[QN]>(cid);                       // (a << 16) | b
-  unsigned short (*iq)[QN] = reinterpret_cast<unsigned short (*)[QN]>(cid + 2 * NW * QN);  // rb * 32 + x
+  uint32_t (*uq)[QN] = reinterpret_cast<uint32_t (*)[QN]>(cid);  // (a << 16) | b
   __shared__ unsigned long long red_epl[NW];
   __shared__ long long red_first[NW], red_last[NW];
   __shared__ unsigned int red_prov[NW];
@@ -288,45 +277,25 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __syncthreads();
 
   // ---- phase 2: unions through per-warp queues
-  int uqn = 0, iqn = 0;  // warp-uniform queue fills
-
-  auto flush_unions = [&](int upto) {
-    // run entries [upto, uqn) in dense rounds of 32
-    __syncwarp();
-    while (uqn > upto) {
-      const int n = uqn - upto < 32 ? uqn - upto : 32;
-      if (lane < n) {
-        const uint32_t e = uq[warp][uqn - n + lane];
-        const int a = (int)(e >> 16), b = (int)(e & 0xFFFFu);
-        if (a >= NODES || b >= NODES) local_err = 2;
-        else if (!sunite(par, (unsigned short)a, (unsigned short)b)) local_err = 1;
-      }
-      uqn -= n;
-      __syncwarp();
-    }
-  };
-  auto push_unions = [&](uint32_t m, unsigned a, unsigned b) {
-    // lanes in m push (a, b); keeps uqn < 32 between calls
-    if (!m) return;
-    if ((m >> lane) & 1u) uq[warp][uqn + __popc(m & lt)] = (a << 16) | (b & 0xFFFFu);
+  int uqn = 0;  // warp-uniform queue fill, below 32 between neighbour rows
+  uint32_t* myq = uq[warp];
+  // lanes in m append (a, b)
+  auto push = [&](uint32_t m, unsigned a, unsigned b) {
+    if ((m >> lane) & 1u) myq[uqn + __popc(m & lt)] = (a << 16) | (b & 0xFFFFu);
     uqn += __popc(m);
-    if (uqn >= 32) flush_unions(uqn - 32 >= 0 ? uqn - 32 : 0);
   };
-  // one item: a voxel whose primary neighbour does not match tests its dx = +-1
-  // neighbours and the halo columns
-  auto flush_items = [&](int upto) {
-    __syncwarp();
-    while (iqn > upto) {
-      const int n = iqn - upto < 32 ? iqn - upto : 32;
-      if (lane < n) {
-        if (tile_item<T, S, CONN, TY, TZ, MODE>(iq[warp][iqn - n + lane], box, smask, par)) local_err = 1;
-      }
-      iqn -= n;
-      __syncwarp();
+  // run whole rounds of 32 from the top of the queue
+  auto flush = [&](int keep) {
+    if (uqn > keep) {
+      const int e = run_unions(myq, keep, uqn, par, NODES, lane);
+      if (e) local_err = e;
+      uqn = keep;
     }
   };
 
-  // tile rows
+  // tile rows.  A union is queued for the first voxel of each pair of runs
+  // (this row's run, the neighbour row's run) that a relation joins; pairs
+  // that a voxel's primary neighbour implies are left out.
   for (int ri = warp; ri < NR; ri += NW) {
     const int rb = box_row_of(ri);
     const S s = sv(rb, lane);
@@ -334,37 +303,26 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     const bool fg = (F >> lane) & 1u;
     const unsigned nR = (unsigned)(ri * 32 + head_of(Sr, lane));
     uint32_t M0[NRN], Sp[NRN];
+    S Wn[NRN];
 #pragma unroll
     for (int k = 0; k < NRN; ++k) {
       int dy, dz, dxs;
       row_nb<CONN>(k, dy, dz, dxs);
       const int rbp = rb + dy + BY * dz;
-      const S w = sv(rbp, lane);
+      Wn[k] = sv(rbp, lane);
       Sp[k] = smask[rbp];
-      M0[k] = __ballot_sync(FULL, fg && rel<MODE>(s, w));
+      M0[k] = __ballot_sync(FULL, fg && rel<MODE>(s, Wn[k]));
     }
     uint32_t SC = 0;
     if (PRI0 >= 0) SC = M0[PRI0 < 0 ? 0 : PRI0];
     if (PRI1 >= 0) SC &= M0[PRI1 < 0 ? 0 : PRI1];
     const uint32_t NEED = (PRI0 >= 0) ? (F & ~SC) : F;
-#pragma unroll
-    for (int k = 0; k < NRN; ++k) {
-      int dy, dz, dxs;
-      row_nb<CONN>(k, dy, dz, dxs);
-      const int rbp = rb + dy + BY * dz;
-      const bool primary = (k == PRI0) || (k == PRI1);
-      uint32_t U = M0[k] & (Sr | Sp[k] | ~(M0[k] << 1));
-      if (!primary) U &= NEED;
-      push_unions(U, nR, node_of(rbp, head_of(Sp[k], lane)));
+    if (HAS_DX && (NEED & 1u)) {
+      // the same row's left neighbour across the x seam
+      const bool r0 = lane == 0 && rel<MODE>(s, sv(rb, -1));
+      push(__ballot_sync(FULL, r0), nR, (unsigned)(CNODE + rb));
     }
-    if (HAS_DX) {
-      // voxels not covered by their primary neighbour become items
-      if (NEED) {
-        if ((NEED >> lane) & 1u) iq[warp][iqn + __popc(NEED & lt)] = (unsigned short)(rb * 32 + lane);
-        iqn += __popc(NEED);
-        if (iqn >= 32) flush_items(iqn - 32 >= 0 ? iqn - 32 : 0);
-      }
-    } else if (F & 1u) {
+    if (!HAS_DX && (F & 1u)) {
       // same-row neighbour across the x seam
       const S s0 = (S)__shfl_sync(FULL, s, 0);
       const S c0 = sv(rb, -1);
@@ -374,11 +332,46 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         const int64_t gy = y0 - 1 + rb % BY;
         r0 = is_fg(c0) && (gy == 0 ? (s0 == c0) : !(is_fg(sv(rb - 1, 0)) && is_fg(sv(rb - 1, -1))));
       } else r0 = is_fg(c0);
-      if (r0) push_unions(1u, (unsigned)(ri * 32), (unsigned)(CNODE + rb));
+      if (r0) push(1u, (unsigned)(ri * 32), (unsigned)(CNODE + rb));
+    }
+#pragma unroll
+    for (int k = 0; k < NRN; ++k) {
+      int dy, dz, dxs;
+      row_nb<CONN>(k, dy, dz, dxs);
+      const int rbp = rb + dy + BY * dz;
+      const bool primary = (k == PRI0) || (k == PRI1);
+      uint32_t U = M0[k] & (Sr | Sp[k] | ~(M0[k] << 1));
+      if (!primary) U &= NEED;
+      if (U) push(U, nR, node_of(rbp, head_of(Sp[k], lane)));
+      if (HAS_DX && NEED) {
+        // Voxels not covered by their primary neighbour relate to the dx = -1
+        // and dx = +1 voxels of the neighbour rows.  The pair (this run, the
+        // neighbour's run) of voxel x repeats that of x - 1 when neither run
+        // starts between them, and it is the dx = 0 pair when the neighbour's
+        // run goes on from x to x -+ 1: both are left out.
+        const uint32_t candL = NEED & ~(M0[k] & ~Sp[k] & ~1u);
+        const uint32_t candR = NEED & ~(M0[k] & ~(Sp[k] >> 1) & 0x7FFFFFFFu);
+        if ((dxs & 1) && candL) {
+          S wl = (S)__shfl_up_sync(FULL, Wn[k], 1);
+          if (lane == 0) wl = sv(rbp, -1);
+          const uint32_t ML = __ballot_sync(FULL, fg && rel<MODE>(s, wl));
+          const uint32_t UL = ML & candL & (Sr | (Sp[k] << 1) | ~(ML << 1));
+          if (UL) push(UL, nR, lane == 0 ? (unsigned)(CNODE + rbp) : node_of(rbp, head_of(Sp[k], lane - 1)));
+        }
+        if ((dxs & 4) && candR) {
+          S wr = (S)__shfl_down_sync(FULL, Wn[k], 1);
+          if (lane == 31) wr = sv(rbp, 32);
+          const uint32_t MR = __ballot_sync(FULL, fg && rel<MODE>(s, wr));
+          const uint32_t UR = MR & candR & (Sr | (Sp[k] >> 1) | 0x80000000u | ~(MR << 1));
+          if (UR)
+            push(UR, nR, lane == 31 ? (unsigned)(CNODE + NRB + rbp) : node_of(rbp, head_of(Sp[k], lane + 1)));
+        }
+      }
+      // at most 1 + 3 * 32 entries were added since the queue held < 32
+      if (uqn >= 32) flush(uqn & 31);
     }
   }
-  flush_items(0);
-  flush_unions(0);
+  flush(0);
   __syncthreads();
 
   // ---- phase 3a: component roots per tile row, run counts per row
