@@ -30,6 +30,7 @@ EXPORTED = (
     "cc3d_gpu_estimate_provisional_label_count",
     "cc3d_gpu_connected_components3d",
     "cc3d_gpu_label_prepare",
+    "cc3d_gpu_label_prepare_continuous",
     "cc3d_gpu_label_finish",
     "cc3d_gpu_special_row",
     "cc3d_gpu_label_minmax",
@@ -99,6 +100,8 @@ def load() -> ctypes.CDLL:
             vp, ci, i64, i64, i64, i64, i64, ctypes.c_double, vp, ci, u64p, ci, ci, ci, vp]
         lib.cc3d_gpu_label_prepare.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, ci, vp,
                                                ctypes.POINTER(Prepared)]
+        lib.cc3d_gpu_label_prepare_continuous.argtypes = [vp, ci, i64, i64, i64, i64, vp, ci, vp,
+                                                          ctypes.POINTER(Prepared)]
         lib.cc3d_gpu_label_finish.argtypes = [ctypes.c_uint64, i64, vp, ci, u64p, ci, vp]
         lib.cc3d_gpu_special_row.argtypes = [vp, ci, ci, i64, i64, i64, i64, vp, ci, u64p, ci, vp]
         lib.cc3d_gpu_label_minmax.argtypes = [vp, ci, ci, i64, u64p, i64p, ci, vp]

@@ -178,6 +178,27 @@ def estimate_provisional_labels(data) -> Tuple[int, int, int]:
     return _epl_call(linear.ctypes.data, _CODE[data.dtype], sx, linear.size, 0, None)
 
 
+_CTYPE_NAME = {1: "uint8_t", 2: "uint16_t", 4: "uint32_t", 8: "uint64_t"}
+
+
+def _delta_element(delta, dtype) -> ctypes.Array:
+    """delta as one element of the type the labeller runs on (the unsigned
+    view of integer data, or the float type), raising the OverflowError that
+    Cython's conversion to that C type raises (cc3d/fastcc3d.pyx:494-608)."""
+    dt = np.dtype(dtype)
+    if dt.kind == "f":
+        raw = np.array([delta], dtype=dt).tobytes()
+    else:
+        width = dt.itemsize
+        d = int(delta)
+        if d < 0:
+            raise OverflowError(f"can't convert negative value to {_CTYPE_NAME[width]}")
+        if d >= 1 << (8 * width):
+            raise OverflowError(f"value too large to convert to {_CTYPE_NAME[width]}")
+        raw = d.to_bytes(width, "little")
+    return ctypes.create_string_buffer(raw, 8)
+
+
 # ---------------------------------------------------------- main entry
 def connected_components(
     data: Any,
@@ -193,9 +214,9 @@ def connected_components(
     """Connected components of a 2D or 3D image, numbered 1..N.
 
     Same signature, return values, dtypes and exceptions as
-    cc3d.connected_components (cc3d/fastcc3d.pyx:244-626).  Continuous-value
-    labelling (``delta`` other than 0 or the dtype's maximum) is not part of
-    this library and raises NotImplementedError."""
+    cc3d.connected_components (cc3d/fastcc3d.pyx:244-626), including
+    continuous-value labelling (``delta`` > 0: neighbours join when their
+    values differ by at most delta; cc3d/cc3d_continuous.hpp:90-392)."""
     is_torch = _is_torch(data)
     on_device = is_torch and data.is_cuda
     if is_torch and not on_device:
@@ -272,9 +293,7 @@ def connected_components(
     else:
         delta = int(delta)
         binary_image = binary0 or (delta == np.iinfo(dtype).max)
-    if delta != 0 and not binary_image:
-        raise NotImplementedError(
-            "continuous-value labelling (delta != 0) is not implemented on the GPU path")
+    continuous = delta != 0 and not binary_image
 
     if on_device:
         stream = dev.stream()
@@ -298,9 +317,14 @@ def connected_components(
 
     # labelling up to the numbering; the same pass computes the estimate
     info = nat.Prepared()
-    nat.check(call(lib.cc3d_gpu_label_prepare, ptr, code, sx, sy, sz, int(connectivity),
-                   int(bool(periodic_boundary)), int(binary_image), mem_in | mem_out_hint, stream,
-                   ctypes.byref(info)))
+    if continuous:
+        dbuf = _delta_element(delta, dtype)
+        nat.check(call(lib.cc3d_gpu_label_prepare_continuous, ptr, code, sx, sy, sz, int(connectivity),
+                       dbuf, mem_in | mem_out_hint, stream, ctypes.byref(info)))
+    else:
+        nat.check(call(lib.cc3d_gpu_label_prepare, ptr, code, sx, sy, sz, int(connectivity),
+                       int(bool(periodic_boundary)), int(binary_image), mem_in | mem_out_hint, stream,
+                       ctypes.byref(info)))
     if binary0:
         epl, first_row, last_row = voxels, 0, sy
     elif binary_image:
@@ -360,6 +384,8 @@ def connected_components(
 
     n = ctypes.c_uint64(0)
     ocode = _OUT_CODE[out_dtype]
+    if not special:
+        _delta_element(delta, dtype)  # the template argument T delta must hold it
     if special:
         # the Cython layer's single-row loop (fastcc3d.pyx:469-470, 644-679)
         is_u64 = int(np.dtype(dtype) == np.uint64)

@@ -362,7 +362,19 @@ int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t
 
 static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                          int64_t connectivity, int periodic_boundary, int binary_image,
-                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant);
+                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant,
+                         bool continuous = false, uint64_t delta_bits = 0);
+
+int cc3d_gpu_label_prepare_continuous(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                                      int64_t connectivity, const void* delta, int mem_flags, void* stream,
+                                      cc3d_gpu_prepared* info) {
+  const size_t isz = dtype_size(dtype);
+  if (!isz || !delta) return fail(CC3D_ERR_INVALID, "invalid arguments");
+  uint64_t bits = 0;
+  memcpy(&bits, delta, isz);
+  return label_prepare(in, dtype, sx, sy, sz, connectivity, 0, 0, mem_flags, stream, info, CC3D_TILE_RUNS,
+                       true, bits);
+}
 
 int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                            int64_t connectivity, int periodic_boundary, int binary_image,
@@ -381,7 +393,8 @@ int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, in
 
 static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                          int64_t connectivity, int periodic_boundary, int binary_image,
-                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant) {
+                         int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant,
+                         bool continuous, uint64_t delta_bits) {
   const size_t isz = dtype_size(dtype);
   if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
   if (sx < 0 || sy < 0 || sz < 0 || !info) return fail(CC3D_ERR_INVALID, "invalid arguments");
@@ -392,6 +405,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
     return fail(CC3D_ERR_RUNTIME, "sz must be 1 for 2D connectivities.");
   if (periodic_boundary && conn != 4 && conn != 8 && conn != 6)
     return fail(CC3D_ERR_INVALID, "periodic_boundary is only implemented for 4, 8 and 6 connectivity");
+  if (continuous && (periodic_boundary || binary_image))
+    return fail(CC3D_ERR_RUNTIME, "periodic_boundary is not currently supported for continuous data.");
   memset(info, 0, sizeof(*info));
   info->first_row = -1;
   info->last_row = -1;
@@ -415,10 +430,15 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   int eff = conn;
   if (sz == 1 && (conn == 26 || conn == 18)) eff = 8;
   if (sz == 1 && conn == 6) eff = 4;
-  const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
+  // continuous values (cc3d/cc3d_continuous.hpp:394-455): the 3D labeller
+  // (any plane count) joins on |a - b| <= delta; the 2D 8-connected one has
+  // its own decision tree
+  const int mode = continuous ? (conn == 8 ? MODE_CONT8Q : MODE_CONT)
+                              : (!binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY));
   const bool block8 = binary_image && conn == 8;
   const bool d3 = (eff == 26 || eff == 18 || eff == 6);
   // tile-pass configuration: the caller's, the autotuned one for this class, or the default
+  if (continuous) variant = CC3D_TILE_RUNS;
   if (variant == CC3D_TILE_AUTO) variant = resolve_tile_pass(dtype, eff, mode, voxels);
   const TileCfg cfg = decode_tile_cfg(variant, d3);
   const int TY = block8 ? 64 : cfg.ty, TZ = block8 ? 1 : cfg.tz, HZ = d3 ? 1 : 0;
@@ -471,6 +491,7 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   const size_t o_pf = cv.take(nwords * sizeof(uint32_t));
   const size_t o_bs = cv.take((nblocks + 1) * sizeof(uint32_t));
   const size_t o_ed = cv.take((size_t)ntiles * a.edge_slots * sizeof(uint2));
+  const size_t o_sp = cv.take(4 * sizeof(unsigned long long));
   // host outputs are staged after the job's buffers (room for uint64 labels)
   job.out_staging_offset = cv.take((mem_flags & CC3D_OUT_DEVICE) ? 0 : voxels * 8);
   if (int rc = reserve(*w, cv.off)) return rc;
@@ -486,6 +507,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   a.bitmap = (uint32_t*)(base + o_bm);
   a.prefix = (uint32_t*)(base + o_pf);
   a.edges = (uint2*)(base + o_ed);
+  a.delta_bits = delta_bits;
+  a.span = (unsigned long long*)(base + o_sp);
   uint32_t* bsum = (uint32_t*)(base + o_bs);
 
   *w->host_ctr = fresh_counters();
@@ -493,7 +516,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   if (block8) CK(cudaMemsetAsync(a.bitmap, 0, nwords * sizeof(uint32_t), s));
   StageTimer tm(*w, s);
   a.in = in;
-  const int nchunks = stage_in ? copy_chunks(a, voxels * (int64_t)isz) : 1;
+  // (the continuous 2D 8-connected pass needs the whole image's span first)
+  const int nchunks = (stage_in && mode != MODE_CONT8Q) ? copy_chunks(a, voxels * (int64_t)isz) : 1;
   if (nchunks > 1) {
     // the input arrives chunk by chunk on the copy stream; the tile pass of a
     // chunk starts once it (and so every chunk before it, whose last plane is
@@ -525,6 +549,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
       a.in = base + o_in;
       tm.mark(0);
     }
+    if (mode == MODE_CONT8Q)
+      CK(DISPATCH_DTYPE(dtype, launch_span, a.in, voxels, (unsigned long long*)a.span, s));
     CK(DISPATCH_DTYPE(dtype, launch_tile_local, a, eff, mode, block8, cfg.variant, ntiles, s));
     tm.mark(2);
   }
@@ -664,12 +690,29 @@ int cc3d_gpu_connected_components3d(const void* in, int dtype, int64_t sx, int64
   if (!N) return fail(CC3D_ERR_INVALID, "invalid arguments");
   if (out_dtype != CC3D_U16 && out_dtype != CC3D_U32 && out_dtype != CC3D_U64)
     return fail(CC3D_ERR_INVALID, "out_dtype must be uint16, uint32 or uint64 (code %d)", out_dtype);
-  if (delta != 0.0 && !binary_image)
-    return fail(CC3D_ERR_UNSUPPORTED, "continuous-value labelling (delta != 0) is not implemented");
   cc3d_gpu_prepared info;
-  if (int rc = cc3d_gpu_label_prepare(in, dtype, sx, sy, sz, connectivity, periodic_boundary,
-                                      binary_image, mem_flags, stream, &info))
+  if (delta != 0.0 && !binary_image) {
+    if (periodic_boundary)
+      return fail(CC3D_ERR_RUNTIME, "periodic_boundary is not currently supported for continuous data.");
+    // delta in the element type, as the template argument T delta
+    unsigned char d[8] = {0};
+    switch (dtype) {
+      case CC3D_U8: { const uint8_t v = (uint8_t)delta; memcpy(d, &v, 1); break; }
+      case CC3D_U16: { const uint16_t v = (uint16_t)delta; memcpy(d, &v, 2); break; }
+      case CC3D_U32: { const uint32_t v = (uint32_t)delta; memcpy(d, &v, 4); break; }
+      case CC3D_U64: { const uint64_t v = (uint64_t)delta; memcpy(d, &v, 8); break; }
+      case CC3D_F32: { const float v = (float)delta; memcpy(d, &v, 4); break; }
+      case CC3D_F64: { memcpy(d, &delta, 8); break; }
+      default: return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
+    }
+    if (delta < 0.0) return fail(CC3D_ERR_INVALID, "delta must be >= 0");
+    if (int rc = cc3d_gpu_label_prepare_continuous(in, dtype, sx, sy, sz, connectivity, d, mem_flags, stream,
+                                                   &info))
+      return rc;
+  } else if (int rc = cc3d_gpu_label_prepare(in, dtype, sx, sy, sz, connectivity, periodic_boundary,
+                                             binary_image, mem_flags, stream, &info)) {
     return rc;
+  }
   return cc3d_gpu_label_finish(info.token, max_labels, out, out_dtype, N, mem_flags & CC3D_OUT_DEVICE,
                                stream);
 }

@@ -243,6 +243,22 @@ cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool blo
                                 int64_t ntiles, cudaStream_t s) {
   const bool d3 = conn == 26 || conn == 18 || conn == 6;
   if (!d3 && (a.ty != 64 || a.tz != 1)) return cudaErrorInvalidValue;
+  if (mode == MODE_CONT8Q) {
+    if (conn != 8) return cudaErrorInvalidValue;
+    return launch_k1_runs<T, 8, 64, 1, MODE_CONT8Q, false>(a, ntiles, s);
+  }
+  if (mode == MODE_CONT) {
+    // continuous values: block-parallel pass, 32 x 8 x 8 tiles
+    if (d3 && (a.ty != 8 || a.tz != 8)) return cudaErrorInvalidValue;
+    switch (conn) {
+      case 26: return launch_k1_runs<T, 26, 8, 8, MODE_CONT, false>(a, ntiles, s);
+      case 18: return launch_k1_runs<T, 18, 8, 8, MODE_CONT, false>(a, ntiles, s);
+      case 6: return launch_k1_runs<T, 6, 8, 8, MODE_CONT, false>(a, ntiles, s);
+      case 8: return launch_k1_runs<T, 8, 64, 1, MODE_CONT, false>(a, ntiles, s);
+      case 4: return launch_k1_runs<T, 4, 64, 1, MODE_CONT, false>(a, ntiles, s);
+    }
+    return cudaErrorInvalidValue;
+  }
   const bool multi = mode == MODE_MULTI;
   switch (conn) {
     case 26:
@@ -312,6 +328,105 @@ cudaError_t launch_minmax_t(const void* in, int64_t n, int is_signed, unsigned l
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ image span
+// The minimum and maximum the reference's continuous 2D 8-connected labeller
+// folds over the whole image with std::min / std::max from element 0
+// (cc3d/cc3d_continuous.hpp:275-280).  For floating point a NaN element makes
+// the running value NaN and the next element replaces it, so the fold equals
+// the plain minimum and maximum of the elements after the last NaN (NaN when
+// the last element is NaN).  res[0], res[1]: minimum and maximum as element
+// bits; res[2]: index of the last NaN (-1 if none); res[3]: scratch.
+template <typename T>
+__device__ __forceinline__ unsigned long long order_key(T v) {
+  if constexpr (std::is_floating_point<T>::value) {
+    using U = typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type;
+    U u;
+    memcpy(&u, &v, sizeof(T));
+    const U sign = U(1) << (8 * sizeof(T) - 1);
+    return (unsigned long long)((u & sign) ? U(~u) : U(u | sign));
+  } else {
+    return (unsigned long long)v;
+  }
+}
+template <typename T>
+__device__ __forceinline__ uint64_t key_bits(unsigned long long k) {
+  if constexpr (std::is_floating_point<T>::value) {
+    using U = typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type;
+    const U sign = U(1) << (8 * sizeof(T) - 1);
+    const U u = (U)k;
+    return (uint64_t)((u & sign) ? U(u & ~sign) : U(~u));
+  } else {
+    return (uint64_t)k;
+  }
+}
+
+template <typename T>
+__global__ void k_span_init(unsigned long long* res) {
+  res[0] = ~0ull;
+  res[1] = 0;
+  res[2] = (unsigned long long)-1ll;
+  res[3] = 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_span_last_nan(const T* in, int64_t n, unsigned long long* res) {
+  long long last = -1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (in[i] != in[i]) last = i;
+  for (int o = 16; o > 0; o >>= 1) last = max(last, (long long)__shfl_down_sync(FULL, last, o));
+  if ((threadIdx.x & 31) == 0 && last >= 0) atomicMax((long long*)&res[2], last);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_span(const T* in, int64_t n, unsigned long long* res) {
+  const int64_t first = (long long)res[2] + 1;
+  unsigned long long kmin = ~0ull, kmax = 0;
+  for (int64_t i = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long k = order_key<T>(in[i]);
+    kmin = k < kmin ? k : kmin;
+    kmax = k > kmax ? k : kmax;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, (unsigned long long)__shfl_down_sync(FULL, kmin, o));
+    kmax = max(kmax, (unsigned long long)__shfl_down_sync(FULL, kmax, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&res[0], kmin);
+    atomicMax(&res[1], kmax);
+  }
+}
+
+template <typename T>
+__global__ void k_span_final(unsigned long long* res, int64_t n) {
+  if constexpr (std::is_floating_point<T>::value) {
+    if ((long long)res[2] + 1 >= n) {
+      // nothing after the last NaN: both folds end in NaN
+      const T nan = T(NAN);
+      uint64_t b = 0;
+      memcpy(&b, &nan, sizeof(T));
+      res[0] = b;
+      res[1] = b;
+      return;
+    }
+  }
+  res[0] = key_bits<T>(res[0]);
+  res[1] = key_bits<T>(res[1]);
+}
+
+template <typename T>
+cudaError_t launch_span_t(const void* in, int64_t n, unsigned long long* res, cudaStream_t s) {
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  const T* p = static_cast<const T*>(in);
+  k_span_init<T><<<1, 1, 0, s>>>(res);
+  if (std::is_floating_point<T>::value) k_span_last_nan<T><<<(unsigned)blocks, 256, 0, s>>>(p, n, res);
+  k_span<T><<<(unsigned)blocks, 256, 0, s>>>(p, n, res);
+  k_span_final<T><<<1, 1, 0, s>>>(res, n);
+  return cudaGetLastError();
+}
+
 }  // namespace cc3dgpu
 
 #define CC3D_DEFINE_DTYPE_LAUNCHERS(SUF, T)                                               \
@@ -335,5 +450,9 @@ cudaError_t launch_minmax_t(const void* in, int64_t n, int is_signed, unsigned l
   cudaError_t launch_minmax_##SUF(const void* in, int64_t n, int is_signed,               \
                                   unsigned long long* res, cudaStream_t s) {              \
     return launch_minmax_t<T>(in, n, is_signed, res, s);                                  \
+  }                                                                                       \
+  cudaError_t launch_span_##SUF(const void* in, int64_t n, unsigned long long* res,       \
+                                cudaStream_t s) {                                         \
+    return launch_span_t<T>(in, n, res, s);                                               \
   }                                                                                       \
   }

@@ -50,7 +50,9 @@ inline bool valid_tile_code(int code) {
                                        int is_uint64, void* out, int out_dtype,        \
                                        Counters* ctr, cudaStream_t s);                \
   cudaError_t launch_minmax_##SUF(const void* in, int64_t voxels, int is_signed,      \
-                                  unsigned long long* res, cudaStream_t s);
+                                  unsigned long long* res, cudaStream_t s);            \
+  cudaError_t launch_span_##SUF(const void* in, int64_t voxels, unsigned long long* res, \
+                                cudaStream_t s);
 
 CC3D_DECLARE_DTYPE_LAUNCHERS(u8)
 CC3D_DECLARE_DTYPE_LAUNCHERS(u16)

@@ -42,6 +42,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace cc3dgpu {
@@ -56,6 +57,8 @@ constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int MODE_MULTI = 0;    // neighbours join when equal and nonzero
 constexpr int MODE_BINARY = 1;   // neighbours join when both nonzero
 constexpr int MODE_BINARY4 = 2;  // the reference's binary 4-connected relation
+constexpr int MODE_CONT = 3;     // continuous values: neighbours join when |a - b| <= delta
+constexpr int MODE_CONT8Q = 4;   // the reference's continuous 2D 8-connected decision tree
 
 // device error bits
 constexpr unsigned ERR_UNITE_BUDGET = 1u;
@@ -131,6 +134,10 @@ struct LabelArgs {
   const uint32_t* tile_vol;    // [tiles] volume of every tile of a batch
   int64_t tile_base;           // first tile of this launch of the tile pass or the writer
   int64_t tile_end;            // one past its last tile
+  // continuous modes: delta as the bits of one input element, and (2D
+  // 8-connected) the image's minimum and maximum as element bits on the device
+  uint64_t delta_bits;
+  const unsigned long long* span;
 };
 
 // Geometry of the volume a tile belongs to, and the tile's place in it.
@@ -208,6 +215,39 @@ template <int MODE, typename S>
 __device__ __forceinline__ bool rel(S a, S b) {
   if (MODE == MODE_MULTI) return a == b;
   return is_fg(b);
+}
+
+// ---------------------------------------------------- continuous values
+// An input element from its bits (the low sizeof(T) bytes).
+template <typename T>
+__host__ __device__ __forceinline__ T from_bits(uint64_t b) {
+  T v;
+  memcpy(&v, &b, sizeof(T));
+  return v;
+}
+
+__device__ __forceinline__ float abs_diff(float a, float b) { return fabsf(a - b); }
+__device__ __forceinline__ double abs_diff(double a, double b) { return fabs(a - b); }
+template <typename T>
+__device__ __forceinline__ T abs_diff(T a, T b) { return a > b ? T(a - b) : T(b - a); }
+
+// |a - b| <= delta in the element type, as cc3d::match
+// (cc3d/cc3d_continuous.hpp:80-88): unsigned without underflow, floating
+// point by the rounded difference (NaN never matches).
+template <typename T>
+__device__ __forceinline__ bool cmatch(T a, T b, T delta) {
+  return abs_diff(a, b) <= delta;
+}
+
+// The 2D 8-connected continuous labeller's second shortcut
+// (cc3d/cc3d_continuous.hpp:301-309): a pixel takes the label above it when
+// both lie within delta of the image's minimum and maximum, whether or not
+// they match each other.  std::min / std::max order, so a NaN operand fails.
+template <typename T>
+__device__ __forceinline__ bool span_shortcut(T cur, T up, T gmin, T gmax, T delta) {
+  const T mn = (up < cur) ? up : cur;
+  const T mx = (cur < up) ? up : cur;
+  return (T)(mn - gmin) <= delta && (T)(gmax - mx) <= delta;
 }
 
 __device__ __forceinline__ uint32_t lanemask_le(int lane) { return (2u << lane) - 1u; }

@@ -113,6 +113,9 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
   constexpr int PRI1 = (CONN == 18) ? 0 : -1;
   constexpr bool HAS_DX = (CONN == 26 || CONN == 18 || CONN == 8);
+  constexpr bool CONT = (MODE == MODE_CONT || MODE == MODE_CONT8Q);
+  constexpr bool EQUAL_JOINS = (MODE == MODE_MULTI || CONT);  // equal neighbours always join
+  static_assert(MODE != MODE_CONT8Q || CONN == 8, "the 2D 8-connected decision tree");
   constexpr int QN = 128;                      // per-warp queue capacity
   static_assert(kTX * NR == kTV, "tile must hold 2048 voxels");
   static_assert(NR == kRowsPerTile, "64 rows per tile");
@@ -161,6 +164,19 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   };
   // stored value of box row rb at tile column x (x in [-1, 32])
   auto sv = [&](int rb, int x) -> S { return to_stored<S, T, MODE>(box[rb * W + PADX + x]); };
+  // relation of a foreground voxel a with a neighbour b
+  const T delta = from_bits<T>(p.delta_bits);
+  auto R = [&](S a, S b) -> bool {
+    if constexpr (CONT) return is_fg(b) && cmatch<T>((T)a, (T)b, delta);
+    else return rel<MODE>(a, b);
+  };
+  // continuous 2D 8-connected: a pixel that takes the label above it and
+  // nothing else (cc3d/cc3d_continuous.hpp:296-309)
+  const T gmin = MODE == MODE_CONT8Q ? from_bits<T>(p.span[0]) : T(0);
+  const T gmax = MODE == MODE_CONT8Q ? from_bits<T>(p.span[1]) : T(0);
+  auto up_only = [&](S a, S up) -> bool {
+    return is_fg(a) && is_fg(up) && (a == up || span_shortcut<T>((T)a, (T)up, gmin, gmax, delta));
+  };
 
   // ---- phase 0: the box arrives (TMA, or plain loads) while the forest is set up
   if (tid == 0) {
@@ -237,6 +253,12 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const bool fg = is_fg(s);
       bool link = lane > 0 && fg && is_fg(sl);
       if (MODE == MODE_MULTI) link = link && (s == sl);
+      if (CONT) link = link && R(s, sl);
+      if (MODE == MODE_CONT8Q) {
+        // a pixel that takes the label above it has no left link; halo rows
+        // keep single-pixel runs (their links depend on rows outside the box)
+        link = link && trow && !up_only(s, sv(rb - 1 < 0 ? 0 : rb - 1, lane));
+      }
       const uint32_t F = __ballot_sync(FULL, fg);
       const uint32_t L = __ballot_sync(FULL, link);
       if (lane == 0) {
@@ -311,15 +333,26 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const int rbp = rb + dy + BY * dz;
       Wn[k] = sv(rbp, lane);
       Sp[k] = smask[rbp];
-      M0[k] = __ballot_sync(FULL, fg && rel<MODE>(s, Wn[k]));
+      M0[k] = __ballot_sync(FULL, fg && R(s, Wn[k]));
     }
     uint32_t SC = 0;
-    if (PRI0 >= 0) SC = M0[PRI0 < 0 ? 0 : PRI0];
-    if (PRI1 >= 0) SC &= M0[PRI1 < 0 ? 0 : PRI1];
+    if (MODE == MODE_CONT8Q) {
+      // the decision tree's first two branches: the pixel above and nothing else
+      SC = __ballot_sync(FULL, up_only(s, Wn[0]));
+      M0[0] |= SC;
+    } else if (CONT) {
+      // an exactly equal primary neighbour stands in for the voxel (equality
+      // carries every match over to it)
+      if (PRI0 >= 0) SC = __ballot_sync(FULL, fg && s == Wn[PRI0 < 0 ? 0 : PRI0]);
+      if (PRI1 >= 0) SC &= __ballot_sync(FULL, fg && s == Wn[PRI1 < 0 ? 0 : PRI1]);
+    } else {
+      if (PRI0 >= 0) SC = M0[PRI0 < 0 ? 0 : PRI0];
+      if (PRI1 >= 0) SC &= M0[PRI1 < 0 ? 0 : PRI1];
+    }
     const uint32_t NEED = (PRI0 >= 0) ? (F & ~SC) : F;
     if (HAS_DX && (NEED & 1u)) {
       // the same row's left neighbour across the x seam
-      const bool r0 = lane == 0 && rel<MODE>(s, sv(rb, -1));
+      const bool r0 = lane == 0 && R(s, sv(rb, -1));
       push(__ballot_sync(FULL, r0), nR, (unsigned)(CNODE + rb));
     }
     if (!HAS_DX && (F & 1u)) {
@@ -328,6 +361,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const S c0 = sv(rb, -1);
       bool r0;
       if (MODE == MODE_MULTI) r0 = (s0 == c0);
+      else if (CONT) r0 = R(s0, c0);
       else if (MODE == MODE_BINARY4) {
         const int64_t gy = y0 - 1 + rb % BY;
         r0 = is_fg(c0) && (gy == 0 ? (s0 == c0) : !(is_fg(sv(rb - 1, 0)) && is_fg(sv(rb - 1, -1))));
@@ -351,17 +385,21 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         // run goes on from x to x -+ 1: both are left out.
         const uint32_t candL = NEED & ~(M0[k] & ~Sp[k] & ~1u);
         const uint32_t candR = NEED & ~(M0[k] & ~(Sp[k] >> 1) & 0x7FFFFFFFu);
+        // voxels whose diagonal relations stand for joins: all of them where
+        // the primary neighbour implies them, only NEED where a voxel that
+        // takes the label above drops its other relations (continuous 2D 8)
+        const bool mine = MODE != MODE_CONT8Q || ((NEED >> lane) & 1u);
         if ((dxs & 1) && candL) {
           S wl = (S)__shfl_up_sync(FULL, Wn[k], 1);
           if (lane == 0) wl = sv(rbp, -1);
-          const uint32_t ML = __ballot_sync(FULL, fg && rel<MODE>(s, wl));
+          const uint32_t ML = __ballot_sync(FULL, fg && mine && R(s, wl));
           const uint32_t UL = ML & candL & (Sr | (Sp[k] << 1) | ~(ML << 1));
           if (UL) push(UL, nR, lane == 0 ? (unsigned)(CNODE + rbp) : node_of(rbp, head_of(Sp[k], lane - 1)));
         }
         if ((dxs & 4) && candR) {
           S wr = (S)__shfl_down_sync(FULL, Wn[k], 1);
           if (lane == 31) wr = sv(rbp, 32);
-          const uint32_t MR = __ballot_sync(FULL, fg && rel<MODE>(s, wr));
+          const uint32_t MR = __ballot_sync(FULL, fg && mine && R(s, wr));
           const uint32_t UR = MR & candR & (Sr | (Sp[k] >> 1) | 0x80000000u | ~(MR << 1));
           if (UR)
             push(UR, nR, lane == 31 ? (unsigned)(CNODE + NRB + rbp) : node_of(rbp, head_of(Sp[k], lane + 1)));
@@ -490,7 +528,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     const int rp = MODE == MODE_BINARY4 ? -1 : prev_row(rb);
     if (rp >= 0) {
       const S a = sv(rb, xi), b = sv(rp, xi);
-      if (is_fg(b) && (MODE == MODE_MULTI ? a == b : true)) {
+      if (is_fg(b) && (EQUAL_JOINS ? a == b : true)) {
         unsigned short np;
         if (xi < 0) np = (unsigned short)(CNODE + rp);
         else if (xi > 31) np = (unsigned short)(CNODE + NRB + rp);

@@ -80,8 +80,10 @@ int cc3d_gpu_estimate_provisional_label_count(
  *                 images, where the reference's union-find is sized from it
  *                 and throws "maximum length exception" when too small -- this
  *                 library reports that case as CC3D_ERR_RUNTIME too.
- *   delta:        must be 0 unless binary_image (continuous labelling,
- *                 cc3d/cc3d_continuous.hpp:90-392, is not implemented).
+ *   delta:        0, or continuous labelling (cc3d/cc3d_continuous.hpp:90-392)
+ *                 with delta converted to the element type (exact for
+ *                 integers below 2^53; cc3d_gpu_label_prepare_continuous takes
+ *                 an element).  Ignored for binary images.
  * Labels are numbered 1..N in raster order of each component's first voxel;
  * binary 8-connected images are numbered in raster order of each component's
  * first 2x2 block, as the reference's block labeller does.  Background is 0.
@@ -121,6 +123,25 @@ int cc3d_gpu_label_prepare(
     const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
     int64_t connectivity, int periodic_boundary, int binary_image,
     int mem_flags, void* stream, cc3d_gpu_prepared* info);
+
+/*
+ * The continuous-value labelling, first step (finish with
+ * cc3d_gpu_label_finish).  Replaces cc3d::connected_components3d<T,OUT> with
+ * delta != 0 (cc3d/cc3d_continuous.hpp:394-455 -> 90-392): neighbours join
+ * when both are foreground and |a - b| <= delta in the element type (unsigned
+ * without underflow; floating point by the rounded difference, so NaN joins
+ * nothing).  26/18/6 use the 3D labeller for any sz; 4 the 2D 4-connected one;
+ * 8 the 2D 8-connected one including its decision tree, where a pixel takes
+ * the label of the pixel above when both lie within delta of the image's
+ * minimum and maximum (cc3d/cc3d_continuous.hpp:296-309).  `delta` points to
+ * one element of the input type.  The result is numbered like every other
+ * path (raster order of each component's first voxel); periodic boundaries
+ * are not supported (CC3D_ERR_RUNTIME, as the reference throws).
+ */
+int cc3d_gpu_label_prepare_continuous(
+    const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
+    int64_t connectivity, const void* delta, int mem_flags, void* stream,
+    cc3d_gpu_prepared* info);
 
 int cc3d_gpu_label_finish(
     uint64_t token, int64_t max_labels, void* out, int out_dtype, uint64_t* N,

@@ -69,7 +69,15 @@ def _lib(kind: str):
         lib.oracle_connected_components.restype = ctypes.c_int
         lib.oracle_epl.argtypes = [ctypes.c_void_p, ctypes.c_int, i64, i64, i64p, i64p]
         lib.oracle_epl.restype = ctypes.c_uint64
+        lib.oracle_connected_components_continuous.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, i64, i64, i64, ctypes.c_int, ctypes.c_void_p,
+            ctypes.c_void_p, ctypes.c_int, u64p]
+        lib.oracle_connected_components_continuous.restype = ctypes.c_int
     else:
+        lib.ref_connected_components_delta.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, i64, i64, i64, i64, i64, ctypes.c_void_p,
+            ctypes.c_void_p, ctypes.c_int, u64p]
+        lib.ref_connected_components_delta.restype = ctypes.c_int
         lib.ref_connected_components.argtypes = [
             ctypes.c_void_p, ctypes.c_int, i64, i64, i64, i64, i64, ctypes.c_void_p,
             ctypes.c_int, u64p, ctypes.c_int, ctypes.c_int]
@@ -258,14 +266,22 @@ def connected_components(data, max_labels=-1, connectivity=26, return_N=False,
         row = data[:, ry, rz] if data.flags.f_contiguous else data[rz, ry, :]
         N = _special_row(row, out[first_row * sx:(first_row + 1) * sx])
     else:
-        if delta != 0 and not binary_image:
-            raise NotImplementedError("continuous (delta != 0) labelling is not part of the oracle")
         cd = _core_dtype(dtype)
         flat = np.ascontiguousarray(_reshape_flat(data).view(cd))
         n = ctypes.c_uint64(0)
         odt = DT_CODES[out_dtype]
         lib = _lib(backend)
-        if backend == "port":
+        dbuf = _delta_bytes(delta, cd)
+        if delta != 0 and not binary_image:
+            if backend == "port":
+                rc = lib.oracle_connected_components_continuous(
+                    flat.ctypes.data, DT_CODES[cd], sx, sy, sz, int(connectivity), dbuf,
+                    out.ctypes.data, odt, ctypes.byref(n))
+            else:
+                rc = lib.ref_connected_components_delta(
+                    flat.ctypes.data, DT_CODES[cd], sx, sy, sz, int(max_labels), int(connectivity),
+                    dbuf, out.ctypes.data, odt, ctypes.byref(n))
+        elif backend == "port":
             rc = lib.oracle_connected_components(
                 flat.ctypes.data, DT_CODES[cd], sx, sy, sz, int(max_labels), int(connectivity),
                 int(bool(binary_image)), int(bool(periodic_boundary)),
@@ -288,6 +304,24 @@ def connected_components(data, max_labels=-1, connectivity=26, return_N=False,
         import torch
         out = torch.from_numpy(out)
     return (out, N) if return_N else out
+
+
+def _delta_bytes(delta, cd: np.dtype):
+    """delta as one element of the labeller's type cd (Cython's conversion at
+    the call, cc3d/fastcc3d.pyx:494-608: OverflowError outside an unsigned
+    type's range)."""
+    cd = np.dtype(cd)
+    if cd.kind == "f":
+        raw = np.array([delta], dtype=cd).tobytes()
+    else:
+        d = int(delta)
+        name = {1: "uint8_t", 2: "uint16_t", 4: "uint32_t", 8: "uint64_t"}[cd.itemsize]
+        if d < 0:
+            raise OverflowError(f"can't convert negative value to {name}")
+        if d >= 1 << (8 * cd.itemsize):
+            raise OverflowError(f"value too large to convert to {name}")
+        raw = d.to_bytes(cd.itemsize, "little")
+    return ctypes.create_string_buffer(raw, 8)
 
 
 def statistics(out_labels: np.ndarray, no_slice_conversion: bool = False) -> dict:

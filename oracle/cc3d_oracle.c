@@ -20,6 +20,11 @@
  *                                        8: cc3d/cc3d.hpp:1377-1418,
  *                                        binary: cc3d/cc3d_binary.hpp:733-758, 938-950,
  *                                        cc3d/cc3d_binary.hpp:1170-1210
+ *       continuous values (delta != 0)   cc3d/cc3d_continuous.hpp:90-392: the 3D labeller
+ *                                        (26/18/6, with its exact-equality shortcut below),
+ *                                        the 2D 4-connected one and the 2D 8-connected one
+ *                                        with its image-span shortcut, restated branch by
+ *                                        branch in oracle_connected_components_continuous
  *       numbering                        cc3d/cc3d.hpp:244-285 (relabel): components are
  *                                        numbered 1..N in raster order of their first voxel;
  *                                        binary 8-connected images use the 2x2-block
@@ -40,6 +45,7 @@
  * background pixels outside each row's foreground span.  This oracle writes 0
  * there, as the GPU path does; foreground pixels match exactly.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -407,6 +413,168 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     store_label(out, out_dtype, i, l ? ren[L.par[l]] : 0);
   }
   (void)fg;
+  free(ren);
+  free(L.par);
+  free(lab);
+  *N = n;
+  return 0;
+}
+
+
+/* ---- continuous values (delta != 0) ------------------------------------ */
+
+/* |a - b| <= delta as cc3d::match (cc3d/cc3d_continuous.hpp:80-88) */
+#define UMATCH(a, b, d) (((a) > (b) ? (a) - (b) : (b) - (a)) <= (d))
+#define FMATCH(a, b, d) (fabsf((a) - (b)) <= (d))
+#define DMATCH(a, b, d) (fabs((a) - (b)) <= (d))
+
+#define DEFINE_CONT(SUF, T, MATCH)                                              \
+/* 3D labeller (cc3d/cc3d_continuous.hpp:90-180): neighbour table of           \
+   compute_neighborhood (:36-76), the first connectivity/2 entries.         */ \
+static void cont3d_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz,      \
+                         int conn, T delta, uint32_t *lab, Labels *L) {        \
+  static const int NB[13][3] = {                                               \
+    {-1,0,0},{0,-1,0},{0,0,-1},{-1,-1,0},{1,-1,0},{0,-1,-1},{0,1,-1},          \
+    {-1,0,-1},{1,0,-1},{-1,-1,-1},{1,-1,-1},{-1,1,-1},{1,1,-1}};               \
+  const int64_t sxy = sx * sy;                                                 \
+  const int nn = conn / 2;                                                     \
+  for (int64_t z = 0; z < sz; z++)                                             \
+    for (int64_t y = 0; y < sy; y++)                                           \
+      for (int64_t x = 0; x < sx; x++) {                                       \
+        const int64_t i = x + sx * (y + sy * z);                               \
+        const T cur = in[i];                                                   \
+        if (cur == 0) { lab[i] = 0; continue; }                                \
+        if (z > 0 && conn == 26 && cur == in[i - sxy]) {                       \
+          lab[i] = lab[i - sxy];                                               \
+          continue;                                                            \
+        }                                                                      \
+        uint32_t c = 0;                                                        \
+        for (int k = 0; k < nn; k++) {                                         \
+          const int64_t nx = x + NB[k][0], ny = y + NB[k][1], nz = z + NB[k][2]; \
+          if (nx < 0 || nx >= sx || ny < 0 || ny >= sy || nz < 0) continue;    \
+          const int64_t j = i + NB[k][0] + sx * NB[k][1] + sxy * NB[k][2];     \
+          const T w = in[j];                                                   \
+          if (w == 0 || !(MATCH(cur, w, delta))) continue;                     \
+          if (c) c = lab_unite(L, c, lab[j]);                                  \
+          else c = lab[j];                                                     \
+        }                                                                      \
+        lab[i] = c ? c : lab_new(L);                                           \
+      }                                                                        \
+}                                                                              \
+/* 2D 4-connected (cc3d/cc3d_continuous.hpp:182-259) */                        \
+static void cont4_##SUF(const T *in, int64_t sx, int64_t sy, T delta,          \
+                        uint32_t *lab, Labels *L) {                            \
+  for (int64_t y = 0; y < sy; y++)                                             \
+    for (int64_t x = 0; x < sx; x++) {                                         \
+      const int64_t i = x + sx * y;                                            \
+      const T cur = in[i];                                                     \
+      if (cur == 0) { lab[i] = 0; continue; }                                  \
+      if (x > 0 && in[i - 1] != 0 && (MATCH(cur, in[i - 1], delta))) {         \
+        lab[i] = lab[i - 1];                                                   \
+        if (y > 0 && cur != in[i - 1 - sx]) {                                  \
+          if (in[i - sx] != 0 && (MATCH(cur, in[i - sx], delta)))              \
+            lab_unite(L, lab[i], lab[i - sx]);                                 \
+        }                                                                      \
+      } else if (y > 0 && in[i - sx] != 0 && (MATCH(cur, in[i - sx], delta))) { \
+        lab[i] = lab[i - sx];                                                  \
+      } else {                                                                 \
+        lab[i] = lab_new(L);                                                   \
+      }                                                                        \
+    }                                                                          \
+}                                                                              \
+/* 2D 8-connected (cc3d/cc3d_continuous.hpp:261-343), with the image's        \
+   minimum and maximum folded by std::min / std::max from element 0         */ \
+static void cont8_##SUF(const T *in, int64_t sx, int64_t sy, T delta,          \
+                        uint32_t *lab, Labels *L) {                            \
+  const int64_t voxels = sx * sy;                                              \
+  T gmax = in[0], gmin = in[0];                                                \
+  for (int64_t i = 1; i < voxels; i++) {                                       \
+    gmax = (in[i] < gmax) ? gmax : in[i];   /* std::max(in[i], gmax) */        \
+    gmin = (gmin < in[i]) ? gmin : in[i];   /* std::min(in[i], gmin) */        \
+  }                                                                            \
+  for (int64_t y = 0; y < sy; y++)                                             \
+    for (int64_t x = 0; x < sx; x++) {                                         \
+      const int64_t i = x + sx * y;                                            \
+      const T cur = in[i];                                                     \
+      if (cur == 0) { lab[i] = 0; continue; }                                  \
+      if (y > 0) {                                                             \
+        const T b = in[i - sx];                                                \
+        if (cur == b) { lab[i] = lab[i - sx]; continue; }                      \
+        if (b != 0) {                                                          \
+          const T mn = (b < cur) ? b : cur, mx = (cur < b) ? b : cur;          \
+          if ((T)(mn - gmin) <= delta && (T)(gmax - mx) <= delta) {            \
+            lab[i] = lab[i - sx];                                              \
+            continue;                                                          \
+          }                                                                    \
+        }                                                                      \
+      }                                                                        \
+      uint32_t c = 0;                                                          \
+      if (y > 0 && in[i - sx] != 0 && (MATCH(cur, in[i - sx], delta))) c = lab[i - sx]; \
+      if (x > 0 && y > 0 && in[i - 1 - sx] != 0 && (MATCH(cur, in[i - 1 - sx], delta))) \
+        c = c ? lab_unite(L, c, lab[i - 1 - sx]) : lab[i - 1 - sx];            \
+      if (x < sx - 1 && y > 0 && in[i + 1 - sx] != 0 && (MATCH(cur, in[i + 1 - sx], delta))) \
+        c = c ? lab_unite(L, c, lab[i + 1 - sx]) : lab[i + 1 - sx];            \
+      if (x > 0 && in[i - 1] != 0 && (MATCH(cur, in[i - 1], delta)))           \
+        c = c ? lab_unite(L, c, lab[i - 1]) : lab[i - 1];                      \
+      lab[i] = c ? c : lab_new(L);                                             \
+    }                                                                          \
+}
+
+DEFINE_CONT(u8, uint8_t, UMATCH)
+DEFINE_CONT(u16, uint16_t, UMATCH)
+DEFINE_CONT(u32, uint32_t, UMATCH)
+DEFINE_CONT(u64, uint64_t, UMATCH)
+DEFINE_CONT(f32, float, FMATCH)
+DEFINE_CONT(f64, double, DMATCH)
+
+/* Continuous-value labelling of `in` (delta: one element of the input type
+ * at `delta`), numbered 1..N in raster order of each component's first
+ * voxel.  Returns 0, -1 on bad arguments, -2 when sz != 1 for a 2D
+ * connectivity, -3 for 2^32 voxels or more, -4 on allocation failure. */
+int oracle_connected_components_continuous(const void *in, int dtype, int64_t sx,
+                                           int64_t sy, int64_t sz, int connectivity,
+                                           const void *delta, void *out, int out_dtype,
+                                           uint64_t *N) {
+  const int (*off)[3];
+  if (offsets_for(connectivity, &off) < 0 || !delta) return -1;
+  if ((connectivity == 8 || connectivity == 4) && sz != 1) return -2;
+  const int64_t voxels = sx * sy * sz;
+  *N = 0;
+  if (voxels == 0) return 0;
+  if (voxels >= (int64_t)0xFFFFFFFFLL) return -3;
+  uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+  if (!lab) return -4;
+  Labels L = {NULL, 0, 0, 0};
+  switch (dtype) {
+#define CASE(D, SUF, T)                                                          \
+    case D: {                                                                    \
+      T d;                                                                       \
+      memcpy(&d, delta, sizeof(T));                                              \
+      if (connectivity == 8) cont8_##SUF((const T *)in, sx, sy, d, lab, &L);     \
+      else if (connectivity == 4) cont4_##SUF((const T *)in, sx, sy, d, lab, &L); \
+      else cont3d_##SUF((const T *)in, sx, sy, sz, connectivity, d, lab, &L);    \
+      break;                                                                     \
+    }
+    CASE(DT_U8, u8, uint8_t)
+    CASE(DT_U16, u16, uint16_t)
+    CASE(DT_U32, u32, uint32_t)
+    CASE(DT_U64, u64, uint64_t)
+    CASE(DT_F32, f32, float)
+    CASE(DT_F64, f64, double)
+#undef CASE
+    default: free(lab); return -1;
+  }
+  if (L.oom) { free(lab); free(L.par); return -4; }
+  for (uint32_t p = 1; p <= L.n; p++) L.par[p] = L.par[L.par[p]];
+  uint32_t *ren = (uint32_t *)calloc((size_t)L.n + 1, sizeof(uint32_t));
+  if (!ren && L.n) { free(lab); free(L.par); return -4; }
+  uint64_t n = 0;
+  for (uint32_t p = 1; p <= L.n; p++)
+    if (L.par[p] == p) ren[p] = (uint32_t)++n;
+  for (int64_t i = 0; i < voxels; i++) {
+    const uint32_t l = lab[i];
+    store_label(out, out_dtype, i, l ? ren[L.par[l]] : 0);
+  }
   free(ren);
   free(L.par);
   free(lab);
