@@ -56,10 +56,6 @@ struct TileBox {
     const int by = rb % BY, bz = rb / BY;
     return by >= 1 && by <= TY && bz >= HZ;
   }
-  __device__ static __forceinline__ unsigned node_of(int rb, int h) {
-    return is_tile_row(rb) ? (unsigned)(((rb % BY - 1) + TY * (rb / BY - HZ)) * 32 + h)
-                           : (unsigned)(HNODE + rb * 32 + h);
-  }
 };
 
 
@@ -140,6 +136,8 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __shared__ unsigned int red_prov[NW];
   __shared__ unsigned int local_err;
   __shared__ unsigned int edge_fill;
+  __shared__ unsigned short nbase[NRB];  // node id of a box row's voxel 0
+  __shared__ unsigned char brow[NR];     // box row of each tile row
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t tile = p.tile_base + blockIdx.x;
@@ -159,9 +157,9 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     const int by = rb % BY, bz = rb / BY;
     return (by == 0 ? 0 : (by == BY - 1 ? 2 : 1)) + 3 * (bz < HZ ? 0 : 1);
   };
-  auto node_of = [&](int rb, int h) -> unsigned {
-    return is_tile_row(rb) ? (unsigned)(tile_row_of(rb) * 32 + h) : (unsigned)(HNODE + rb * 32 + h);
-  };
+  // the box row of tile row ri, from the table filled in phase 0
+  auto box_row = [&](int ri) -> int { return brow[ri]; };
+  static_assert(NRB < 256, "box rows fit a byte");
   // stored value of box row rb at tile column x (x in [-1, 32])
   auto sv = [&](int rb, int x) -> S { return to_stored<S, T, MODE>(box[rb * W + PADX + x]); };
   // relation of a foreground voxel a with a neighbour b
@@ -211,6 +209,9 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       }
     }
   }
+  for (int rb = tid; rb < NRB; rb += kThreads)
+    nbase[rb] = (unsigned short)(is_tile_row(rb) ? tile_row_of(rb) * 32 : HNODE + rb * 32);
+  for (int ri = tid; ri < NR; ri += kThreads) brow[ri] = (unsigned char)box_row_of(ri);
   {
     // identity forest, four nodes per store
     uint2* p4 = reinterpret_cast<uint2*>(par);
@@ -319,7 +320,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // (this row's run, the neighbour row's run) that a relation joins; pairs
   // that a voxel's primary neighbour implies are left out.
   for (int ri = warp; ri < NR; ri += NW) {
-    const int rb = box_row_of(ri);
+    const int rb = box_row(ri);
     const S s = sv(rb, lane);
     const uint32_t F = fmask[rb], Sr = smask[rb];
     const bool fg = (F >> lane) & 1u;
@@ -376,7 +377,8 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const bool primary = (k == PRI0) || (k == PRI1);
       uint32_t U = M0[k] & (Sr | Sp[k] | ~(M0[k] << 1));
       if (!primary) U &= NEED;
-      if (U) push(U, nR, node_of(rbp, head_of(Sp[k], lane)));
+      const unsigned nb = nbase[rbp];
+      if (U) push(U, nR, nb + head_of(Sp[k], lane));
       if (HAS_DX && NEED) {
         // Voxels not covered by their primary neighbour relate to the dx = -1
         // and dx = +1 voxels of the neighbour rows.  The pair (this run, the
@@ -394,7 +396,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
           if (lane == 0) wl = sv(rbp, -1);
           const uint32_t ML = __ballot_sync(FULL, fg && mine && R(s, wl));
           const uint32_t UL = ML & candL & (Sr | (Sp[k] << 1) | ~(ML << 1));
-          if (UL) push(UL, nR, lane == 0 ? (unsigned)(CNODE + rbp) : node_of(rbp, head_of(Sp[k], lane - 1)));
+          if (UL) push(UL, nR, lane == 0 ? (unsigned)(CNODE + rbp) : nb + head_of(Sp[k], lane - 1));
         }
         if ((dxs & 4) && candR) {
           S wr = (S)__shfl_down_sync(FULL, Wn[k], 1);
@@ -402,7 +404,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
           const uint32_t MR = __ballot_sync(FULL, fg && mine && R(s, wr));
           const uint32_t UR = MR & candR & (Sr | (Sp[k] >> 1) | 0x80000000u | ~(MR << 1));
           if (UR)
-            push(UR, nR, lane == 31 ? (unsigned)(CNODE + NRB + rbp) : node_of(rbp, head_of(Sp[k], lane + 1)));
+            push(UR, nR, lane == 31 ? (unsigned)(CNODE + NRB + rbp) : nb + head_of(Sp[k], lane + 1));
         }
       }
       // at most 1 + 3 * 32 entries were added since the queue held < 32
@@ -414,7 +416,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
 
   // ---- phase 3a: component roots per tile row, run counts per row
   for (int ri = warp; ri < NR; ri += NW) {
-    const int rb = box_row_of(ri);
+    const int rb = box_row(ri);
     const uint32_t Sr = smask[rb];
     bool root = false;
     if ((Sr >> lane) & 1u) {
@@ -460,7 +462,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // ---- phase 3b: run records, keys, bitmap
   const uint32_t node0 = (uint32_t)(tile * kTV);
   for (int ri = warp; ri < NR; ri += NW) {
-    const int rb = box_row_of(ri);
+    const int rb = box_row(ri);
     const uint32_t Sr = smask[rb], F = fmask[rb];
     const int ly = ri % TY, lz = ri / TY;
     const int64_t y = y0 + ly, z = z0 + lz;
@@ -575,7 +577,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       // 2x2 blocks Y Z / X W; C D E F in the row above, B A to the left
       for (int q = tid; q < kTV / 4; q += kThreads) {
         const int b = q & 15, ri = 2 * (q >> 4);
-        const int rb = box_row_of(ri);
+        const int rb = box_row(ri);
         const uint32_t Fa = fmask[rb - 1], F0 = fmask[rb], F1 = fmask[rb + 1];
         const uint32_t ca = colfg(rb - 1, -1), c0 = colfg(rb, -1);
         const uint32_t c1 = colfg(rb + 1, -1), ra = colfg(rb - 1, 32);
@@ -593,7 +595,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       }
     } else {
       for (int ri = warp; ri < NR; ri += NW) {
-        const int rb = box_row_of(ri);
+        const int rb = box_row(ri);
         const uint32_t F = fmask[rb];
         const S s = sv(rb, lane);
         uint32_t Lk;
