@@ -232,7 +232,9 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
 
   // ---- masks of every box row, epl on the tile's own rows
   unsigned long long epl_acc = 0;
-  long long frow = 0x7FFFFFFFFFFFFFFFLL, lrow = -1;
+  // first and last box rows with foreground runs (box-row order is raster
+  // order for rows inside the volume); -1 / NRB when none
+  int frb = NRB, lrb = -1;
   for (int rb = warp; rb < NRB; rb += NW) {
     const int by = rb % BY, bz = rb / BY;
     const T v = box[rb * W + PADX + lane];
@@ -243,9 +245,8 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const unsigned m = __ballot_sync(FULL, (v != prev) && (v != T(0)));
       if (m) {
         epl_acc += __popc(m);
-        const long long rg = (long long)((y0 - 1 + by) + g.sy * (z0 - HZ + bz));
-        frow = rg < frow ? rg : frow;
-        lrow = rg > lrow ? rg : lrow;
+        frb = rb < frb ? rb : frb;
+        lrb = rb > lrb ? rb : lrb;
       }
     }
     if (MODE != MODE_BINARY4) {
@@ -624,9 +625,11 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
 
   // ---- reductions
   if (lane == 0) {
+    // global row index y + sy * z of a box row
+    auto grow = [&](int rb) -> long long { return (y0 - 1 + rb % BY) + g.sy * (z0 - HZ + rb / BY); };
     red_epl[warp] = epl_acc;
-    red_first[warp] = frow;
-    red_last[warp] = lrow;
+    red_first[warp] = frb < NRB ? grow(frb) : 0x7FFFFFFFFFFFFFFFLL;
+    red_last[warp] = lrb >= 0 ? grow(lrb) : -1;
   }
   unsigned int pw = prov;
 #pragma unroll
