@@ -185,3 +185,38 @@ def test_repeatable_under_concurrency(cc3d):
         out, N = cc3d.connected_components(devb, connectivity=6, binary_image=True, return_N=True)
         assert N == expb[1]
         assert np.array_equal(out.cpu().numpy(), expb[0])
+
+
+TMA_DTYPES = [np.uint8, np.uint16, np.uint32, np.uint64, np.float32, np.float64]
+
+
+@pytest.mark.parametrize("dtype", TMA_DTYPES)
+def test_tma_box_edges(cc3d, dtype):
+    """Rows whose byte length is a multiple of 16 take the TMA box copy: x
+    extents that end inside a tile, volumes narrower than the box padding,
+    single planes and rows; each against the oracle, plus the same volume at a
+    base address that is not 16-byte aligned (plain loads)."""
+    import torch
+    per16 = 16 // np.dtype(dtype).itemsize
+    rng = np.random.default_rng(per16 * 7 + np.dtype(dtype).itemsize)
+    shapes = [(5, 9, per16), (3, 11, 3 * per16), (4, 17, 2 * 32 + per16), (2, 3, 32), (1, 70, 5 * per16),
+              (9, 1, 32 + per16), (1, 1, 64)]
+    for shape in shapes:
+        for conn in (26, 18, 6):
+            a = (rng.integers(1, 4, shape) * (rng.random(shape) < 0.7)).astype(dtype)
+            _compare(cc3d.connected_components, a, dict(connectivity=conn))
+            _compare(cc3d.connected_components, a, dict(connectivity=conn, binary_image=True))
+            _compare(cc3d.connected_components, a, dict(connectivity=conn, delta=1))
+        plane = a[0]
+        for conn in (8, 4):
+            _compare(cc3d.connected_components, plane, dict(connectivity=conn))
+            _compare(cc3d.connected_components, plane, dict(connectivity=conn, delta=1))
+            _compare(cc3d.connected_components, plane, dict(connectivity=conn, periodic_boundary=True))
+        # the same volume on the device at a base 1 element past an aligned one
+        flat = torch.zeros(a.size + 1, dtype=getattr(torch, np.dtype(dtype).name), device="cuda")
+        flat[1:] = torch.from_numpy(a.reshape(-1)).cuda()
+        t = flat[1:].view(a.shape)
+        assert t.data_ptr() % 16 != 0
+        got, n = cc3d.connected_components(t, connectivity=26, return_N=True)
+        exp, en = oracle.connected_components(a, connectivity=26, return_N=True)
+        assert n == en and np.array_equal(got.cpu().numpy(), exp)

@@ -28,7 +28,9 @@ def test_choice_follows_the_thread_setting(cc3d):
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "scan/8x8"
     cc3d.set_tile_pass("auto")
     cc3d.autotune_reset()
-    assert cc3d.tile_pass_choice(vol) == "runs/8x8"  # the default without tuning data
+    # the defaults without tuning data
+    assert cc3d.tile_pass_choice(vol) == "runs/16x4"
+    assert cc3d.tile_pass_choice(vol, connectivity=6) == "runs/8x8"
     # binary 8-connected images always take the block pass (2x2-block numbering)
     cc3d.set_tile_pass("scan")
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs/8x8"
