@@ -14,7 +14,11 @@ write of the uint32 output.  Inputs are synthetic and seeded.
            larger than L2 (129 MB), so no flush is needed between steps.
     e2e    the same metric through the C ABI with pinned host buffers: the
            host->device copy of the input and the device->host copy of the
-           labels are inside the timed region.
+           labels are inside the timed region.  Two host threads take
+           alternate volumes (the library keeps a workspace and stream per
+           thread), so one volume's copy-out overlaps the next one's copy-in
+           and tile pass; the single-thread figure is reported beside it.
+           Median of three K-step runs, every run listed.
 --impl reference
     The reference's CPU implementation of the path on this machine's host
     cores: the compiled reference where it was built here (oracle/_ref), else
@@ -27,6 +31,7 @@ path has no data exchange), value = all voxels / max over ranks of the time.
 from __future__ import annotations
 
 import argparse
+import concurrent.futures
 import ctypes
 import json
 import os
@@ -248,6 +253,10 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+E2E_THREADS = 2  # host threads of the end-to-end leg
+E2E_REPS = 3     # timed K-step runs of the end-to-end leg (median reported)
+
+
 def run_gpu(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -308,9 +317,9 @@ def run_gpu(args, world, rank, local):
     host_in = pin_in.numpy()
     osz = {torch.uint16: 2, torch.uint32: 4, torch.uint64: 8}[out_dtype]
     ocode = {2: nat.U16, 4: nat.U32, 8: nat.U64}[osz]
-    pin_out = torch.empty(voxels * osz, dtype=torch.uint8).pin_memory()
+    pin_outs = [torch.empty(voxels * osz, dtype=torch.uint8).pin_memory() for _ in range(E2E_THREADS)]
 
-    def e2e_step():
+    def e2e_step(pin_out):
         # prepare (input staged once; the estimate comes from the same pass),
         # then write the labels into the pinned host buffer
         info = nat.Prepared()
@@ -321,23 +330,58 @@ def run_gpu(args, world, rank, local):
                                             ocode, ctypes.byref(n), 0, None))
         return n.value
 
-    e2e_value = None
-    e2e_stages = None
-    if not args.skip_e2e:
-        for _ in range(args.warmup):
-            e2e_step()
-        barrier(world)
+    # persistent host threads: the library keeps one device workspace per
+    # thread, so the same threads serve the warm-up and the timed steps
+    pool = concurrent.futures.ThreadPoolExecutor(E2E_THREADS)
+    gate = threading.Barrier(E2E_THREADS)
+
+    def e2e_run(nsteps, nthreads):
+        # nthreads > 1: volumes alternate between the pool's threads; each
+        # labels its share one volume at a time through the C ABI (its own
+        # workspace and stream), so one volume's label copy-out overlaps the
+        # next one's copy-in and tile pass.  nthreads == 1: the calling thread.
+        def worker(t):
+            torch.cuda.set_device(local)
+            gate.wait()  # every pool thread takes one share
+            return [e2e_step(pin_outs[t]) for _ in range(t, nsteps, nthreads)]
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            assert e2e_step() == N
-        t_e2e = max_over_ranks(world, time.perf_counter() - t0)
-        e2e_value = world * voxels * args.steps / t_e2e / 1e9
+        if nthreads == 1:
+            ns = [e2e_step(pin_outs[0]) for _ in range(nsteps)]
+        else:
+            futs = [pool.submit(worker, t) for t in range(nthreads)]
+            ns = [n for f in futs for n in f.result()]
+        dt = time.perf_counter() - t0
+        assert all(n == N for n in ns), "e2e N differs from the device path"
+        return dt
+
+    e2e_value = e2e_single = None
+    e2e_stages = None
+    reps_multi, reps_single = [], []
+    if not args.skip_e2e:
+        # every thread's workspace allocated and warm before timing
+        e2e_run(max(args.warmup, 1) * E2E_THREADS, E2E_THREADS)
+        e2e_run(max(args.warmup, 1), 1)
+        # The host side of these copies is shared with other tenants of the
+        # machine, so the K-step run is repeated (alternating with the
+        # single-thread run) and the median reported, every repetition listed.
+        reps_multi, reps_single = [], []
+        for _ in range(E2E_REPS):
+            barrier(world)
+            t_e2e = max_over_ranks(world, e2e_run(args.steps, E2E_THREADS))
+            reps_multi.append(world * voxels * args.steps / t_e2e / 1e9)
+            barrier(world)
+            t_one = max_over_ranks(world, e2e_run(args.steps, 1))
+            reps_single.append(world * voxels * args.steps / t_one / 1e9)
+        e2e_value = pystats.median(reps_multi)
+        e2e_single = pystats.median(reps_single)
         expect = out.cpu().numpy().reshape(-1).view(np.uint8)
-        assert np.array_equal(pin_out.numpy(), expect), "e2e labels differ from the device path"
+        for t in range(min(E2E_THREADS, args.steps)):
+            assert np.array_equal(pin_outs[t].numpy(), expect), "e2e labels differ from the device path"
+        pool.shutdown()
         # one more (untimed) step with the stage timer: where the end-to-end time goes
         nat.profile_enable(True)
         nat.profile_read()
-        e2e_step()
+        e2e_step(pin_outs[0])
         e2e_stages = {k: v[0] for k, v in nat.profile_read().items() if v[1]}
         nat.profile_enable(False)
 
@@ -378,8 +422,15 @@ def run_gpu(args, world, rank, local):
                    "l2": "input (512 MiB) larger than L2, no flush"},
         "e2e": {"value": e2e_value, "unit": "GVoxels/s",
                 "h2d_bytes_per_step": voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
-                "path": "C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish), pinned host buffers; "
-                        "input and labels cross in 8 chunks overlapped with the tile pass and the writer",
+                "path": f"C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish) per volume, pinned host "
+                        f"buffers, {E2E_THREADS} host threads taking alternate volumes (each with its own "
+                        "workspace and stream, so one volume's label copy-out overlaps the next one's "
+                        "copy-in and tile pass); within a call input and labels cross in 8 chunks "
+                        "overlapped with the tile pass and the writer",
+                "repetitions": {"runs": E2E_REPS, "steps_each": args.steps,
+                                "values": reps_multi if e2e_value is not None else None,
+                                "single_thread_values": reps_single if e2e_value is not None else None},
+                "single_thread_value": e2e_single,
                 "stage_ms": e2e_stages},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
