@@ -262,10 +262,12 @@ int resolve_tile_pass(int dtype, int eff, int mode, int64_t voxels) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(dtype, eff, mode, size_bucket(voxels)));
   if (it != g_tuned.end()) return it->second;
-  // without tuning data: block-parallel pass; 32 x 16 x 4 tiles for the 18-
-  // and 26-connected neighbourhoods (fewer halo planes per voxel), 32 x 8 x 8
-  // for 6 (measured on 512^3 volumes: 3-5 % either way)
-  return (eff == 26 || eff == 18) ? (CC3D_TILE_RUNS | CC3D_TILE_16x4) : CC3D_TILE_RUNS;
+  // without tuning data: block-parallel pass; 32 x 16 x 4 tiles for large
+  // volumes at 18/26-connectivity (fewer halo planes per voxel: 3-5 % on
+  // 512^3), 32 x 8 x 8 otherwise (small volumes waste less of a 16-row tile;
+  // on a stream of 16-256 edged volumes 8 x 8 is 1.3x faster)
+  return ((eff == 26 || eff == 18) && voxels >= (int64_t(1) << 24)) ? (CC3D_TILE_RUNS | CC3D_TILE_16x4)
+                                                                    : CC3D_TILE_RUNS;
 }
 }  // namespace
 

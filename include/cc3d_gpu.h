@@ -272,7 +272,8 @@ int cc3d_gpu_run_starts_copy(uint64_t* positions, uint64_t* labels, uint64_t nst
  *
  * cc3d_gpu_set_tile_pass: the calling thread's configuration (CC3D_TILE_AUTO
  *   = the autotuned choice for the volume's class, else RUNS | 16x4 for
- *   18/26-connectivity and RUNS | 8x8 otherwise); returns
+ *   volumes of 2^24 voxels or more at 18/26-connectivity and RUNS | 8x8
+ *   otherwise); returns
  *   the previous setting, or CC3D_ERR_INVALID for an unknown code.
  * cc3d_gpu_tile_pass_choice: the configuration a labelling of this volume
  *   would use now.

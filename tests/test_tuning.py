@@ -28,9 +28,12 @@ def test_choice_follows_the_thread_setting(cc3d):
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "scan/8x8"
     cc3d.set_tile_pass("auto")
     cc3d.autotune_reset()
-    # the defaults without tuning data
-    assert cc3d.tile_pass_choice(vol) == "runs/16x4"
-    assert cc3d.tile_pass_choice(vol, connectivity=6) == "runs/8x8"
+    # the defaults without tuning data: 32x16x4 tiles for large 18/26-connected volumes
+    assert cc3d.tile_pass_choice(vol) == "runs/8x8"
+    big = np.zeros((256, 256, 256), np.uint8)
+    assert cc3d.tile_pass_choice(big) == "runs/16x4"
+    assert cc3d.tile_pass_choice(big, connectivity=18) == "runs/16x4"
+    assert cc3d.tile_pass_choice(big, connectivity=6) == "runs/8x8"
     # binary 8-connected images always take the block pass (2x2-block numbering)
     cc3d.set_tile_pass("scan")
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs/8x8"
