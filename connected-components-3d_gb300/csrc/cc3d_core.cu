@@ -205,14 +205,12 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
 
 // ---------------------------------------------------------------- writer
 template <typename OUT>
+cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s);
+
+template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
   k_resolve<<<152 * 16, 256, 0, s>>>(a);
-  if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)ntiles, kThreads, 0, s>>>(a, out);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  return launch_write_tiles_t<OUT>(a, out, ntiles, s);
 }
 
 // ------------------------------------------------------------ batches
@@ -286,6 +284,8 @@ cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
 // the writer alone, for the tiles [a.tile_base, a.tile_base + count)
 template <typename OUT>
 cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  // one block per tile (a resident grid walking the tiles measured slower)
   if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
   else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
   else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);

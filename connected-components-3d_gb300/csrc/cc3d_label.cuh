@@ -161,11 +161,14 @@ __device__ __forceinline__ TileGeo tile_geo(const LabelArgs& p, int64_t tile) {
     g.in = p.in; g.sx = p.sx; g.sy = p.sy; g.sz = p.sz; g.ntx = p.ntx; g.nty = p.nty;
     g.wpr = p.wpr; g.key_row = p.key_row; g.tile0 = 0; g.word0 = 0;
   }
-  const int64_t local = tile - g.tile0;
-  g.tx = (int)(local % g.ntx);
-  const int64_t rest = local / g.ntx;
-  g.ty = (int)(rest % g.nty);
-  g.tz = (int)(rest / g.nty);
+  // tile indices of a volume fit 32 bits (node ids do), so 32-bit division
+  const uint32_t local = (uint32_t)(tile - g.tile0);
+  const uint32_t ntx = (uint32_t)g.ntx, nty = (uint32_t)g.nty;
+  const uint32_t rest = local / ntx;
+  g.tx = (int)(local - rest * ntx);
+  const uint32_t tz = rest / nty;
+  g.ty = (int)(rest - tz * nty);
+  g.tz = (int)tz;
   return g;
 }
 
