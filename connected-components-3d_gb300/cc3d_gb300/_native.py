@@ -31,6 +31,8 @@ EXPORTED = (
     "cc3d_gpu_connected_components3d",
     "cc3d_gpu_label_prepare",
     "cc3d_gpu_label_prepare_continuous",
+    "cc3d_gpu_voxel_connectivity_graph",
+    "cc3d_gpu_label_prepare_graph",
     "cc3d_gpu_label_finish",
     "cc3d_gpu_special_row",
     "cc3d_gpu_label_minmax",
@@ -103,6 +105,9 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_label_prepare_continuous.argtypes = [vp, ci, i64, i64, i64, i64, vp, ci, vp,
                                                           ctypes.POINTER(Prepared)]
         lib.cc3d_gpu_label_finish.argtypes = [ctypes.c_uint64, i64, vp, ci, u64p, ci, vp]
+        lib.cc3d_gpu_voxel_connectivity_graph.argtypes = [vp, ci, i64, i64, i64, ci, vp, vp]
+        lib.cc3d_gpu_label_prepare_graph.argtypes = [vp, ci, i64, i64, i64, i64, ci, vp,
+                                                     ctypes.POINTER(Prepared)]
         lib.cc3d_gpu_special_row.argtypes = [vp, ci, ci, i64, i64, i64, i64, vp, ci, u64p, ci, vp]
         lib.cc3d_gpu_label_minmax.argtypes = [vp, ci, ci, i64, u64p, i64p, ci, vp]
         lib.cc3d_gpu_statistics.argtypes = [vp, ci, i64, i64, i64, ci, ci, ctypes.c_uint64, vp, vp, ci, vp, ci, vp]

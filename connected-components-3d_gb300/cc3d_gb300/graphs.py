@@ -184,3 +184,118 @@ def each(labels: np.ndarray, binary: bool = False, in_place: bool = False):
                 draw(0, rns, img)
 
     return InPlaceImageIterator() if in_place else ImageIterator()
+
+
+_VCG_INPUT = {np.dtype(np.bool_): 1, np.dtype(np.uint8): 1, np.dtype(np.int8): 1, np.dtype(np.uint16): 2,
+              np.dtype(np.int16): 2, np.dtype(np.uint32): 4, np.dtype(np.int32): 4, np.dtype(np.uint64): 8,
+              np.dtype(np.int64): 8}
+
+
+def _f_order_device(data):
+    """(flat CUDA tensor of `data` in F order -- axis 0 fastest --, numpy dtype, shape)."""
+    import torch
+    if _is_torch(data):
+        t = data if data.is_cuda else data.cuda()
+        npd = np.dtype(str(t.dtype).replace("torch.", ""))
+        flat = t.permute(*reversed(range(t.dim()))).contiguous().reshape(-1)
+        return flat, npd, tuple(t.shape)
+    a = np.asarray(data)
+    flat = np.asfortranarray(a).reshape(-1, order="F")
+    return torch.from_numpy(np.ascontiguousarray(flat)).cuda(), a.dtype, a.shape
+
+
+def _from_f_order(flat, shape, like_torch: bool):
+    """A flat F-ordered CUDA tensor back as an array of `shape` (numpy F order,
+    or a CUDA tensor view with F strides)."""
+    if like_torch:
+        return flat.view(*reversed(shape)).permute(*reversed(range(len(shape))))
+    return flat.cpu().numpy().reshape(shape, order="F")
+
+
+def voxel_connectivity_graph(data: Any, connectivity: int = 26):
+    """Bitfield of the directions in which each voxel's neighbour has the same
+    label (cc3d/fastcc3d.pyx:1021-1178; cc3d/cc3d_graphs.hpp:31-240): uint8
+    for 4, 8 and 6-connectivity, uint32 for 18 and 26.  Axes are the array's
+    own (x = axis 0), as in the reference; a bit stays set at the volume's
+    faces.  CUDA tensors give CUDA tensors."""
+    from .api import DimensionError
+    import torch
+    dims = len(data.shape)
+    if dims not in (1, 2, 3):
+        raise DimensionError("Only 1D, 2D, and 3D arrays supported. Got: " + str(dims))
+    if dims == 2 and connectivity not in (4, 8, 6, 18, 26):
+        raise ValueError("Only 4, 8, and 6, 18, 26 connectivities are supported for 2D images. Got: "
+                         + str(connectivity))
+    elif dims != 2 and connectivity not in (6, 18, 26):
+        raise ValueError("Only 6, 18, and 26 connectivities are supported for 3D images. Got: "
+                         + str(connectivity))
+    out_dtype = np.dtype(np.uint8) if connectivity in (4, 8, 6) else np.dtype(np.uint32)
+    is_t = _is_torch(data)
+    n = int(np.prod(data.shape))
+    if n == 0:
+        if is_t:
+            return torch.zeros((0,), dtype=getattr(torch, out_dtype.name), device=data.device)
+        return np.zeros(shape=(0,), dtype=out_dtype)
+    npd = np.dtype(str(data.dtype).replace("torch.", "")) if is_t else np.asarray(data).dtype
+    if npd not in _VCG_INPUT:
+        raise TypeError("Type {} not currently supported.".format(npd))
+    flat, _, shape = _f_order_device(data)
+    shape3 = tuple(shape) + (1,) * (3 - dims)
+    sx, sy, sz = (int(v) for v in shape3)
+    width = _VCG_INPUT[npd]  # labels compare as unsigned integers of this width
+    out = torch.empty((n,), dtype=getattr(torch, out_dtype.name), device=flat.device)
+    lib = nat.load()
+    with torch.cuda.device(flat.device):
+        nat.check(lib.cc3d_gpu_voxel_connectivity_graph(
+            flat.data_ptr(), width, sx, sy, sz, int(connectivity), out.data_ptr(),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return _from_f_order(out, tuple(shape), is_t)
+
+
+def color_connectivity_graph(vcg: Any, connectivity: int = 26, return_N: bool = False):
+    """Connected components of a voxel connectivity graph (uint8 or uint32
+    bitfields in the layout voxel_connectivity_graph produces), as uint32
+    labels 1..N; every voxel is a node and joins a backward neighbour where its
+    own bit says so.  Mirrors cc3d.color_connectivity_graph
+    (cc3d/fastcc3d.pyx:941-1019; cc3d/cc3d_graphs.hpp:558-1105), including
+    its argument errors and its use of the 2D bit layout for a single plane.
+    CUDA tensors give CUDA tensors."""
+    from .api import DimensionError
+    import torch
+    dims = len(vcg.shape)
+    if dims not in (2, 3):
+        raise DimensionError("Only 2D, and 3D arrays supported. Got: " + str(dims))
+    if dims == 2 and connectivity not in [4, 8, 6, 26]:
+        raise ValueError(f"Only 4 and 8 connectivity is supported for 2D images. Got: {connectivity}")
+    elif dims != 2 and connectivity not in [6, 26]:
+        raise ValueError(f"Only 6 and 26 connectivity are supported for 3D images. Got: {connectivity}")
+    is_t = _is_torch(vcg)
+    npd = np.dtype(str(vcg.dtype).replace("torch.", "")) if is_t else np.asarray(vcg).dtype
+    if npd not in [np.uint8, np.uint32]:
+        raise ValueError(f"Only uint8 and uint32 are supported. Got: {npd}")
+    n = int(np.prod(vcg.shape))
+    if n == 0:
+        if is_t:
+            out = torch.zeros([0] * dims, dtype=torch.uint32, device=vcg.device)
+        else:
+            out = np.zeros([0] * dims, dtype=np.uint32, order="F")
+        return (out, 0) if return_N else out
+    shape3 = tuple(vcg.shape) + (1,) * (3 - dims)
+    sx, sy, sz = (int(v) for v in shape3)
+    if connectivity in [18, 26] and sz > 1 and npd != np.uint32:
+        raise ValueError(f"Only uint32 is supported for 18 and 26 connected. Got: {npd}")
+    flat, _, shape = _f_order_device(vcg)
+    lib = nat.load()
+    out = torch.empty((n,), dtype=torch.uint32, device=flat.device)
+    cnt = ctypes.c_uint64(0)
+    with torch.cuda.device(flat.device):
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        info = nat.Prepared()
+        nat.check(lib.cc3d_gpu_label_prepare_graph(flat.data_ptr(), nat.U8 if npd == np.uint8 else nat.U32,
+                                                   sx, sy, sz, int(connectivity),
+                                                   nat.IN_DEVICE | nat.OUT_DEVICE, stream, ctypes.byref(info)))
+        nat.check(lib.cc3d_gpu_label_finish(info.token, n, out.data_ptr(), nat.U32, ctypes.byref(cnt),
+                                            nat.OUT_DEVICE, stream))
+    labels = _from_f_order(out, tuple(shape), is_t)
+    N = int(cnt.value)
+    return (labels, N) if return_N else labels

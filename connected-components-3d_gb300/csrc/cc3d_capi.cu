@@ -368,7 +368,21 @@ int cc3d_gpu_estimate_provisional_label_count(const void* in, int dtype, int64_t
 static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                          int64_t connectivity, int periodic_boundary, int binary_image,
                          int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant,
-                         bool continuous = false, uint64_t delta_bits = 0);
+                         bool continuous = false, uint64_t delta_bits = 0, bool graph = false);
+
+int cc3d_gpu_label_prepare_graph(const void* vcg, int dtype, int64_t sx, int64_t sy, int64_t sz,
+                                 int64_t connectivity, int mem_flags, void* stream, cc3d_gpu_prepared* info) {
+  if (dtype != CC3D_U8 && dtype != CC3D_U32)
+    return fail(CC3D_ERR_INVALID, "voxel connectivity graphs are uint8 or uint32 (dtype code %d)", dtype);
+  const int c = (int)connectivity;
+  if (c != 26 && c != 6 && c != 4 && c != 8)
+    return fail(CC3D_ERR_RUNTIME, "Only 4, 8, 6 and 26 connectivities are supported.");
+  if (sz > 1 && c != 6 && c != 26) return fail(CC3D_ERR_RUNTIME, "Only 6 and 26 connectivity is supported in 3D.");
+  // one plane: the 2D labellers (4 for 4 and 6, 8 for 8 and 26)
+  const int64_t conn = sz == 1 ? ((c == 4 || c == 6) ? 4 : 8) : c;
+  return label_prepare(vcg, dtype, sx, sy, sz, conn, 0, 0, mem_flags, stream, info, CC3D_TILE_RUNS, false, 0,
+                       true);
+}
 
 int cc3d_gpu_label_prepare_continuous(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                                       int64_t connectivity, const void* delta, int mem_flags, void* stream,
@@ -399,7 +413,7 @@ int cc3d_gpu_label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, in
 static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                          int64_t connectivity, int periodic_boundary, int binary_image,
                          int mem_flags, void* stream, cc3d_gpu_prepared* info, int variant,
-                         bool continuous, uint64_t delta_bits) {
+                         bool continuous, uint64_t delta_bits, bool graph) {
   const size_t isz = dtype_size(dtype);
   if (!isz) return fail(CC3D_ERR_INVALID, "unknown dtype code %d", dtype);
   if (sx < 0 || sy < 0 || sz < 0 || !info) return fail(CC3D_ERR_INVALID, "invalid arguments");
@@ -438,12 +452,13 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   // continuous values (cc3d/cc3d_continuous.hpp:394-455): the 3D labeller
   // (any plane count) joins on |a - b| <= delta; the 2D 8-connected one has
   // its own decision tree
-  const int mode = continuous ? (conn == 8 ? MODE_CONT8Q : MODE_CONT)
+  const int mode = graph ? MODE_GRAPH
+                 : continuous ? (conn == 8 ? MODE_CONT8Q : MODE_CONT)
                               : (!binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY));
   const bool block8 = binary_image && conn == 8;
   const bool d3 = (eff == 26 || eff == 18 || eff == 6);
   // tile-pass configuration: the caller's, the autotuned one for this class, or the default
-  if (continuous) variant = CC3D_TILE_RUNS;
+  if (continuous || graph) variant = CC3D_TILE_RUNS;
   if (variant == CC3D_TILE_AUTO) variant = resolve_tile_pass(dtype, eff, mode, voxels);
   const TileCfg cfg = decode_tile_cfg(variant, d3);
   const int TY = block8 ? 64 : cfg.ty, TZ = block8 ? 1 : cfg.tz, HZ = d3 ? 1 : 0;
@@ -478,7 +493,7 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   a.ntiles = ntiles;
   a.tile_base = 0;
   a.tile_end = ntiles;
-  a.want_epl = binary_image ? 0 : 1;
+  a.want_epl = (binary_image || graph) ? 0 : 1;
   a.want_prov = binary_image ? 1 : 0;
 
   const bool stage_in = !(mem_flags & CC3D_IN_DEVICE);

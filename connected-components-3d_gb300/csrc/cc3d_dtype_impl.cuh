@@ -243,6 +243,18 @@ cudaError_t launch_tile_local_t(const LabelArgs& a, int conn, int mode, bool blo
                                 int64_t ntiles, cudaStream_t s) {
   const bool d3 = conn == 26 || conn == 18 || conn == 6;
   if (!d3 && (a.ty != 64 || a.tz != 1)) return cudaErrorInvalidValue;
+  if (mode == MODE_GRAPH) {
+    // voxel connectivity graphs are uint8 or uint32 bitfields
+    if constexpr (std::is_same<T, uint8_t>::value || std::is_same<T, uint32_t>::value) {
+      switch (conn) {
+        case 26: return launch_k1_runs<T, 26, 8, 8, MODE_GRAPH, false>(a, ntiles, s);
+        case 6: return launch_k1_runs<T, 6, 8, 8, MODE_GRAPH, false>(a, ntiles, s);
+        case 8: return launch_k1_runs<T, 8, 64, 1, MODE_GRAPH, false>(a, ntiles, s);
+        case 4: return launch_k1_runs<T, 4, 64, 1, MODE_GRAPH, false>(a, ntiles, s);
+      }
+    }
+    return cudaErrorInvalidValue;
+  }
   if (mode == MODE_CONT8Q) {
     if (conn != 8) return cudaErrorInvalidValue;
     return launch_k1_runs<T, 8, 64, 1, MODE_CONT8Q, false>(a, ntiles, s);

@@ -59,6 +59,8 @@ constexpr int MODE_BINARY = 1;   // neighbours join when both nonzero
 constexpr int MODE_BINARY4 = 2;  // the reference's binary 4-connected relation
 constexpr int MODE_CONT = 3;     // continuous values: neighbours join when |a - b| <= delta
 constexpr int MODE_CONT8Q = 4;   // the reference's continuous 2D 8-connected decision tree
+constexpr int MODE_GRAPH = 5;    // a voxel connectivity graph: every voxel is a node, and it
+                                 // joins a backward neighbour where its own bit says so
 
 // device error bits
 constexpr unsigned ERR_UNITE_BUDGET = 1u;
@@ -218,6 +220,23 @@ template <int MODE, typename S>
 __device__ __forceinline__ bool rel(S a, S b) {
   if (MODE == MODE_MULTI) return a == b;
   return is_fg(b);
+}
+
+// ------------------------------------------- voxel connectivity graphs
+// Bit (0-based) of direction (dx, dy, dz) in a 3D voxel connectivity graph:
+// faces +x -x +y -y +z -z, then edges and corners in the order of
+// cc3d/cc3d_graphs.hpp:81-96; -1 for the centre.
+__host__ __device__ __forceinline__ int dir_bit3(int dx, int dy, int dz) {
+  constexpr signed char t[27] = {
+      25, 17, 24, 15, 5, 14, 23, 16, 22,   // dz = -1
+      9, 3, 8, 1, -1, 0, 7, 2, 6,          // dz = 0
+      21, 13, 20, 11, 4, 10, 19, 12, 18};  // dz = +1
+  return t[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
+}
+// 2D graphs: +x -x +y -y, then xy, -xy, x-y, -x-y (cc3d/cc3d_graphs.hpp:25-29)
+__host__ __device__ __forceinline__ int dir_bit2(int dx, int dy) {
+  constexpr signed char t[9] = {7, 3, 6, 1, -1, 0, 5, 2, 4};
+  return t[(dx + 1) + 3 * (dy + 1)];
 }
 
 // ---------------------------------------------------- continuous values

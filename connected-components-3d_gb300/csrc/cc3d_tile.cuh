@@ -106,8 +106,10 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
   // neighbour rows (indices into row_nb) whose dx = 0 match makes a voxel's
   // other backward relations implied; -1 = none
-  constexpr int PRI0 = (CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1));
-  constexpr int PRI1 = (CONN == 18) ? 0 : -1;
+  // (a connectivity graph implies nothing: every relation is its own bit)
+  constexpr bool GRAPH = MODE == MODE_GRAPH;
+  constexpr int PRI0 = GRAPH ? -1 : ((CONN == 26) ? 2 : (CONN == 18 ? 2 : (CONN == 8 ? 0 : -1)));
+  constexpr int PRI1 = (!GRAPH && CONN == 18) ? 0 : -1;
   constexpr bool HAS_DX = (CONN == 26 || CONN == 18 || CONN == 8);
   constexpr bool CONT = (MODE == MODE_CONT || MODE == MODE_CONT8Q);
   constexpr bool EQUAL_JOINS = (MODE == MODE_MULTI || CONT);  // equal neighbours always join
@@ -137,6 +139,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __shared__ unsigned int local_err;
   __shared__ unsigned int edge_fill;
   __shared__ unsigned short nbase[NRB];  // node id of a box row's voxel 0
+  __shared__ unsigned char vcol[GRAPH ? NRB : 1];  // graphs: bit 0 / 1: column x0-1 / x0+32 in the volume
   __shared__ unsigned char brow[NR];     // box row of each tile row
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -174,6 +177,13 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const T gmax = MODE == MODE_CONT8Q ? from_bits<T>(p.span[1]) : T(0);
   auto up_only = [&](S a, S up) -> bool {
     return is_fg(a) && is_fg(up) && (a == up || span_shortcut<T>((T)a, (T)up, gmin, gmax, delta));
+  };
+  // graphs: the bit of voxel value a for direction (dx, dy, dz); a single
+  // plane reads uint8 graphs in the 2D layout and uint32 graphs in the 3D one
+  // (the two 8-connected labellers, cc3d/cc3d_graphs.hpp:831-1017)
+  auto gbit = [&](S a, int dx, int dy, int dz) -> bool {
+    const int b = (D3 || sizeof(T) == 4) ? dir_bit3(dx, dy, dz) : dir_bit2(dx, dy);
+    return ((uint32_t)a >> b) & 1u;
   };
 
   // ---- phase 0: the box arrives (TMA, or plain loads) while the forest is set up
@@ -249,7 +259,20 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         lrb = rb > lrb ? rb : lrb;
       }
     }
-    if (MODE != MODE_BINARY4) {
+    if (GRAPH) {
+      // every voxel inside the volume is a node; it links to its left
+      // neighbour where its own -x bit is set
+      const int64_t gy = y0 - 1 + by, gz = z0 - HZ + bz;
+      const bool rowin = gy >= 0 && gy < g.sy && gz >= 0 && gz < g.sz;
+      const bool in = rowin && x0 + lane < g.sx;
+      const uint32_t F = __ballot_sync(FULL, in);
+      const uint32_t L = __ballot_sync(FULL, in && lane > 0 && gbit((S)v, -1, 0, 0));
+      if (lane == 0) {
+        fmask[rb] = F;
+        smask[rb] = F & ~L;
+        vcol[GRAPH ? rb : 0] = (unsigned char)((rowin && x0 > 0 ? 1 : 0) | (rowin && x0 + kTX < g.sx ? 2 : 0));
+      }
+    } else if (MODE != MODE_BINARY4) {
       const S s = to_stored<S, T, MODE>(v);
       const S sl = (S)__shfl_up_sync(FULL, s, 1);
       const bool fg = is_fg(s);
@@ -335,7 +358,8 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const int rbp = rb + dy + BY * dz;
       Wn[k] = sv(rbp, lane);
       Sp[k] = smask[rbp];
-      M0[k] = __ballot_sync(FULL, fg && R(s, Wn[k]));
+      if (GRAPH) M0[k] = __ballot_sync(FULL, fg && gbit(s, 0, dy, dz) && ((fmask[rbp] >> lane) & 1u));
+      else M0[k] = __ballot_sync(FULL, fg && R(s, Wn[k]));
     }
     uint32_t SC = 0;
     if (MODE == MODE_CONT8Q) {
@@ -354,7 +378,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     const uint32_t NEED = (PRI0 >= 0) ? (F & ~SC) : F;
     if (HAS_DX && (NEED & 1u)) {
       // the same row's left neighbour across the x seam
-      const bool r0 = lane == 0 && R(s, sv(rb, -1));
+      const bool r0 = lane == 0 && (GRAPH ? (gbit(s, -1, 0, 0) && (vcol[GRAPH ? rb : 0] & 1u)) : R(s, sv(rb, -1)));
       push(__ballot_sync(FULL, r0), nR, (unsigned)(CNODE + rb));
     }
     if (!HAS_DX && (F & 1u)) {
@@ -362,7 +386,8 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const S s0 = (S)__shfl_sync(FULL, s, 0);
       const S c0 = sv(rb, -1);
       bool r0;
-      if (MODE == MODE_MULTI) r0 = (s0 == c0);
+      if (GRAPH) r0 = gbit(s0, -1, 0, 0) && (vcol[GRAPH ? rb : 0] & 1u);
+      else if (MODE == MODE_MULTI) r0 = (s0 == c0);
       else if (CONT) r0 = R(s0, c0);
       else if (MODE == MODE_BINARY4) {
         const int64_t gy = y0 - 1 + rb % BY;
@@ -395,14 +420,20 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         if ((dxs & 1) && candL) {
           S wl = (S)__shfl_up_sync(FULL, Wn[k], 1);
           if (lane == 0) wl = sv(rbp, -1);
-          const uint32_t ML = __ballot_sync(FULL, fg && mine && R(s, wl));
+          const bool rl = GRAPH ? (gbit(s, -1, dy, dz) && (lane > 0 ? ((fmask[rbp] >> (lane - 1)) & 1u)
+                                                                     : (vcol[GRAPH ? rbp : 0] & 1u)))
+                                : R(s, wl);
+          const uint32_t ML = __ballot_sync(FULL, fg && mine && rl);
           const uint32_t UL = ML & candL & (Sr | (Sp[k] << 1) | ~(ML << 1));
           if (UL) push(UL, nR, lane == 0 ? (unsigned)(CNODE + rbp) : nb + head_of(Sp[k], lane - 1));
         }
         if ((dxs & 4) && candR) {
           S wr = (S)__shfl_down_sync(FULL, Wn[k], 1);
           if (lane == 31) wr = sv(rbp, 32);
-          const uint32_t MR = __ballot_sync(FULL, fg && mine && R(s, wr));
+          const bool rr = GRAPH ? (gbit(s, 1, dy, dz) && (lane < 31 ? ((fmask[rbp] >> (lane + 1)) & 1u)
+                                                                     : ((vcol[GRAPH ? rbp : 0] >> 1) & 1u)))
+                                : R(s, wr);
+          const uint32_t MR = __ballot_sync(FULL, fg && mine && rr);
           const uint32_t UR = MR & candR & (Sr | (Sp[k] >> 1) | 0x80000000u | ~(MR << 1));
           if (UR)
             push(UR, nR, lane == 31 ? (unsigned)(CNODE + NRB + rbp) : nb + head_of(Sp[k], lane + 1));
@@ -524,14 +555,24 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       gx = x0 + xi;
       lx = (int)(gx & 31);
       node = (unsigned short)(CNODE + c);
-      if (!is_fg(sv(rb, xi))) return false;
+      if (GRAPH ? !((vcol[GRAPH ? rb : 0] >> (c < NRB ? 0 : 1)) & 1u) : !is_fg(sv(rb, xi))) return false;
     }
     const unsigned short r = sfind_ro(par, node);
     if (r >= kTV) return false;
     const int rp = MODE == MODE_BINARY4 ? -1 : prev_row(rb);
     if (rp >= 0) {
       const S a = sv(rb, xi), b = sv(rp, xi);
-      if (is_fg(b) && (EQUAL_JOINS ? a == b : true)) {
+      // joined inside their own tile: equal values, or (graphs) the later
+      // voxel's bit towards the earlier one, with both in the volume
+      bool joined;
+      if (GRAPH) {
+        const bool rp_in = xi < 0 ? (vcol[GRAPH ? rp : 0] & 1u) : (xi > 31 ? ((vcol[GRAPH ? rp : 0] >> 1) & 1u)
+                                                                           : ((fmask[rp] >> xi) & 1u));
+        joined = rp_in && (rp == rb - 1 ? gbit(a, 0, -1, 0) : gbit(a, 0, 0, -1));
+      } else {
+        joined = is_fg(b) && (EQUAL_JOINS ? a == b : true);
+      }
+      if (joined) {
         unsigned short np;
         if (xi < 0) np = (unsigned short)(CNODE + rp);
         else if (xi > 31) np = (unsigned short)(CNODE + NRB + rp);

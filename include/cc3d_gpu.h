@@ -143,6 +143,23 @@ int cc3d_gpu_label_prepare_continuous(
     int64_t connectivity, const void* delta, int mem_flags, void* stream,
     cc3d_gpu_prepared* info);
 
+/*
+ * Connected components of a voxel connectivity graph, first step (finish with
+ * cc3d_gpu_label_finish, uint32 output).  Replaces color_connectivity_graph_N
+ * (cc3d/cc3d_graphs.hpp:1077-1105, bound at cc3d/fastcc3d.pyx:941-1019):
+ * every voxel is a node, and a voxel joins a backward neighbour (inside the
+ * volume) when its own bit for that direction is set, so an asymmetric graph
+ * follows the later voxel's bits as the reference does.  `vcg` is uint8 or
+ * uint32 (dtype CC3D_U8 / CC3D_U32).  With sz > 1 connectivity is 6 or 26 (3D
+ * bit layout); a single plane is 4-connected for 4 and 6 and 8-connected for
+ * 8 and 26, reading uint8 graphs in the 2D layout and uint32 graphs in the 3D
+ * one, as the reference's two 8-connected labellers do.  Components are numbered 1..N in raster order of
+ * their first voxel.
+ */
+int cc3d_gpu_label_prepare_graph(
+    const void* vcg, int dtype, int64_t sx, int64_t sy, int64_t sz,
+    int64_t connectivity, int mem_flags, void* stream, cc3d_gpu_prepared* info);
+
 int cc3d_gpu_label_finish(
     uint64_t token, int64_t max_labels, void* out, int out_dtype, uint64_t* N,
     int mem_flags, void* stream);
@@ -425,6 +442,21 @@ int cc3d_gpu_connected_components3d_noalloc(
     int64_t max_labels, int64_t connectivity,
     void* out, int out_dtype, uint64_t* N,
     int periodic_boundary, int binary_image, void* stream);
+
+/*
+ * The voxel connectivity graph of a labelled volume (device pointers): per
+ * voxel a bitfield of the directions whose neighbour lies in the volume with
+ * the same label or lies outside it.  Replaces
+ * extract_voxel_connectivity_graph<T,OUT> (cc3d/cc3d_graphs.hpp:31-240,
+ * bound at cc3d/fastcc3d.pyx:1021-1178).  `labels` holds sx*sy*sz unsigned
+ * integers of label_bytes (1, 2, 4, 8) with x fastest; `graph` receives uint8
+ * fields for connectivity 4, 8 and 6 and uint32 fields for 18 and 26 (bit
+ * layout of the reference: 2D +x -x +y -y xy -xy x-y -x-y; 3D faces, edges,
+ * corners).  4 and 8 need sz == 1.  Synchronises `stream`.
+ */
+int cc3d_gpu_voxel_connectivity_graph(
+    const void* labels, int label_bytes, int64_t sx, int64_t sy, int64_t sz,
+    int connectivity, void* graph, void* stream);
 
 #ifdef __cplusplus
 }
