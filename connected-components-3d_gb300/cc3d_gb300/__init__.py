@@ -16,6 +16,7 @@ from .tuning import autotune, autotune_reset, set_tile_pass, tile_pass_choice  #
 from .batch import autotune_batch, connected_components_batch  # noqa: F401
 from . import costmodel, tuning  # noqa: F401
 from .filters import dust, largest_k  # noqa: F401
+from .stack import LabelStack, connected_components_stack  # noqa: F401
 from .graphs import (  # noqa: F401
     color_connectivity_graph, contacts, draw, each, region_graph, runs, voxel_connectivity_graph)
 
@@ -40,4 +41,6 @@ __all__ = [
     "tile_pass_choice",
     "voxel_connectivity_graph",
     "color_connectivity_graph",
+    "connected_components_stack",
+    "LabelStack",
 ]
