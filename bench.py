@@ -509,6 +509,45 @@ def run_all_configs(args):
                           "variants": res}), flush=True)
 
 
+# ------------------------------------------------------------ connectivity graphs
+def run_graphs(args):
+    """Device-resident voxel_connectivity_graph (a stencil: one read of the
+    labels, one write of the bitfield) and color_connectivity_graph on the
+    headline volume; one JSON line per function."""
+    import torch
+    import cc3d_gb300 as cc3d
+    cc3d.build()
+    peak, peak_kind = load_peaks()
+    vol = make_volume(0)
+    dev = torch.from_numpy(vol).cuda()
+    voxels = vol.size
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(args.steps):
+            r = fn()
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps, r
+
+    ms, vcg = timed(lambda: cc3d.voxel_connectivity_graph(dev, connectivity=26))
+    nbytes = voxels * (vol.itemsize + 4)
+    print(json.dumps({"metric": "GVoxels/s voxel_connectivity_graph 512^3 uint32, 26-connected (uint32 bits)",
+                      "value": voxels / ms / 1e6, "unit": "GVoxels/s", "ms_per_step": ms,
+                      "steps": args.steps, "warmup": args.warmup,
+                      "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak, "unit": "GB/s",
+                                   "frac": nbytes / ms / 1e6 / peak, "peak_source": peak_kind,
+                                   "algorithmic_bytes_per_step": nbytes}}), flush=True)
+    ms, res = timed(lambda: cc3d.color_connectivity_graph(vcg, connectivity=26, return_N=True))
+    print(json.dumps({"metric": "GVoxels/s color_connectivity_graph 512^3 (uint32 graph of the volume), 26",
+                      "value": voxels / ms / 1e6, "unit": "GVoxels/s", "ms_per_step": ms,
+                      "steps": args.steps, "warmup": args.warmup, "N": int(res[1])}), flush=True)
+
+
 # ------------------------------------------------------------ batched stream
 def run_batch(args):
     """The mixed-size stream: N uint16 Voronoi+membrane volumes, every edge
@@ -628,6 +667,8 @@ def main():
                     help="one line per benchmarked workload and tile-pass variant instead of the headline")
     ap.add_argument("--batch", type=int, default=0,
                     help="the mixed-size stream of this many volumes instead of the headline")
+    ap.add_argument("--graphs", action="store_true",
+                    help="voxel and colour connectivity graphs of the headline volume instead of the headline")
     ap.add_argument("--costmodel", type=int, default=0,
                     help="train and judge the cost model on this many generated volumes instead of the headline")
     ap.add_argument("--save-params", default="", help="where --costmodel saves the trained parameters")
@@ -646,6 +687,9 @@ def main():
         return
     if args.batch:
         run_batch(args)
+        return
+    if args.graphs:
+        run_graphs(args)
         return
     if args.costmodel:
         run_costmodel(args)

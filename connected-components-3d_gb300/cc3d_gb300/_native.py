@@ -105,7 +105,7 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_label_prepare_continuous.argtypes = [vp, ci, i64, i64, i64, i64, vp, ci, vp,
                                                           ctypes.POINTER(Prepared)]
         lib.cc3d_gpu_label_finish.argtypes = [ctypes.c_uint64, i64, vp, ci, u64p, ci, vp]
-        lib.cc3d_gpu_voxel_connectivity_graph.argtypes = [vp, ci, i64, i64, i64, ci, vp, vp]
+        lib.cc3d_gpu_voxel_connectivity_graph.argtypes = [vp, ci, i64, i64, i64, ci, ci, vp, vp]
         lib.cc3d_gpu_label_prepare_graph.argtypes = [vp, ci, i64, i64, i64, i64, ci, vp,
                                                      ctypes.POINTER(Prepared)]
         lib.cc3d_gpu_special_row.argtypes = [vp, ci, ci, i64, i64, i64, i64, vp, ci, u64p, ci, vp]

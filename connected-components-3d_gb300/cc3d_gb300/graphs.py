@@ -239,17 +239,33 @@ def voxel_connectivity_graph(data: Any, connectivity: int = 26):
     npd = np.dtype(str(data.dtype).replace("torch.", "")) if is_t else np.asarray(data).dtype
     if npd not in _VCG_INPUT:
         raise TypeError("Type {} not currently supported.".format(npd))
-    flat, _, shape = _f_order_device(data)
-    shape3 = tuple(shape) + (1,) * (3 - dims)
-    sx, sy, sz = (int(v) for v in shape3)
+    shape = tuple(int(v) for v in data.shape)
+    # C-ordered arrays are read in place with the axes reversed (the kernel
+    # maps memory offsets back to the reference's x = axis 0); anything else
+    # goes through a Fortran-ordered copy
+    if is_t:
+        t = data if data.is_cuda else data.cuda()
+        rev = dims > 1 and t.is_contiguous()
+        flat = t.reshape(-1) if rev else t.permute(*reversed(range(dims))).contiguous().reshape(-1)
+    else:
+        a = np.asarray(data)
+        rev = dims > 1 and a.flags.c_contiguous and not a.flags.f_contiguous
+        host = np.ascontiguousarray(a).reshape(-1) if rev else np.asfortranarray(a).reshape(-1, order="F")
+        flat = torch.from_numpy(np.ascontiguousarray(host)).cuda()
+    ext = tuple(reversed(shape)) if rev else shape
+    sx, sy, sz = (int(v) for v in ext + (1,) * (3 - dims))
     width = _VCG_INPUT[npd]  # labels compare as unsigned integers of this width
     out = torch.empty((n,), dtype=getattr(torch, out_dtype.name), device=flat.device)
     lib = nat.load()
     with torch.cuda.device(flat.device):
         nat.check(lib.cc3d_gpu_voxel_connectivity_graph(
-            flat.data_ptr(), width, sx, sy, sz, int(connectivity), out.data_ptr(),
+            flat.data_ptr(), width, sx, sy, sz, int(connectivity), dims if rev else 0, out.data_ptr(),
             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
-    return _from_f_order(out, tuple(shape), is_t)
+    if rev:
+        if is_t:
+            return out.view(*shape)
+        return np.asfortranarray(out.cpu().numpy().reshape(shape))
+    return _from_f_order(out, shape, is_t)
 
 
 def color_connectivity_graph(vcg: Any, connectivity: int = 26, return_N: bool = False):

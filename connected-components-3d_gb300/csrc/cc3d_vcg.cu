@@ -35,7 +35,11 @@ int failf(int code, const char* fmt, ...) {
 constexpr int VX = 32, VY = 8, VZ = 8;                  // voxels per block
 constexpr int BXW = VX + 2, BYW = VY + 2, BZW = VZ + 2;  // staged box with halo
 
-template <typename T, typename OUT, bool D3>
+// REV: the array is C-ordered, so memory runs its last axis fastest: with
+// REV = 3 (3D arrays) memory offsets (a, b, c) are the field's directions
+// (x, y, z) = (c, b, a); with REV = 2 (2D arrays) (x, y, z) = (b, a, c).
+// sx, sy, sz are the memory extents, fastest first.
+template <typename T, typename OUT, bool D3, int REV>
 __global__ void __launch_bounds__(VX * VY) k_vcg(const T* __restrict__ in, int64_t sx, int64_t sy, int64_t sz,
                                                  OUT* __restrict__ out, uint32_t mask, int64_t nbx, int64_t nby) {
   __shared__ T box[BZW][BYW][BXW];
@@ -75,7 +79,8 @@ __global__ void __launch_bounds__(VX * VY) k_vcg(const T* __restrict__ in, int64
             const bool exists = (dx < 0 ? xm : (dx > 0 ? xp : true)) && (dy < 0 ? ym : (dy > 0 ? yp : true)) &&
                                 (dz < 0 ? zm : (dz > 0 ? zp : true));
             const bool differs = exists && box[lz + 1 + dz][ty + 1 + dy][tx + 1 + dx] != cur;
-            if (!differs) bits |= 1u << dir_bit3(dx, dy, dz);
+            if (!differs)
+              bits |= 1u << (REV == 3 ? dir_bit3(dz, dy, dx) : REV == 2 ? dir_bit3(dy, dx, dz) : dir_bit3(dx, dy, dz));
           }
     } else {
 #pragma unroll
@@ -85,7 +90,7 @@ __global__ void __launch_bounds__(VX * VY) k_vcg(const T* __restrict__ in, int64
           if (!dx && !dy) continue;
           const bool exists = (dx < 0 ? xm : (dx > 0 ? xp : true)) && (dy < 0 ? ym : (dy > 0 ? yp : true));
           const bool differs = exists && box[1][ty + 1 + dy][tx + 1 + dx] != cur;
-          if (!differs) bits |= 1u << dir_bit2(dx, dy);
+          if (!differs) bits |= 1u << (REV ? dir_bit2(dy, dx) : dir_bit2(dx, dy));
         }
     }
     out[(z * sy + y) * sx + x] = (OUT)(bits & mask);
@@ -93,33 +98,41 @@ __global__ void __launch_bounds__(VX * VY) k_vcg(const T* __restrict__ in, int64
 }
 
 template <typename T, typename OUT, bool D3>
-void launch_vcg(const void* in, int64_t sx, int64_t sy, int64_t sz, void* out, uint32_t mask, cudaStream_t s) {
+void launch_vcg(const void* in, int64_t sx, int64_t sy, int64_t sz, void* out, uint32_t mask, int rev,
+                cudaStream_t s) {
   const int64_t nbx = (sx + VX - 1) / VX, nby = (sy + VY - 1) / VY, nbz = (sz + VZ - 1) / VZ;
-  k_vcg<T, OUT, D3><<<(unsigned)(nbx * nby * nbz), dim3(VX, VY), 0, s>>>(
-      static_cast<const T*>(in), sx, sy, sz, static_cast<OUT*>(out), mask, nbx, nby);
+  const unsigned grid = (unsigned)(nbx * nby * nbz);
+  const T* i = static_cast<const T*>(in);
+  OUT* o = static_cast<OUT*>(out);
+  if (rev == 3) k_vcg<T, OUT, D3, 3><<<grid, dim3(VX, VY), 0, s>>>(i, sx, sy, sz, o, mask, nbx, nby);
+  else if (rev == 2) k_vcg<T, OUT, D3, 2><<<grid, dim3(VX, VY), 0, s>>>(i, sx, sy, sz, o, mask, nbx, nby);
+  else k_vcg<T, OUT, D3, 0><<<grid, dim3(VX, VY), 0, s>>>(i, sx, sy, sz, o, mask, nbx, nby);
 }
 
 template <typename T>
-void launch_vcg_t(const void* in, int64_t sx, int64_t sy, int64_t sz, int conn, void* out, cudaStream_t s) {
+void launch_vcg_t(const void* in, int64_t sx, int64_t sy, int64_t sz, int conn, void* out, int rev,
+                  cudaStream_t s) {
   // 2D fields for 4 / 8 (one plane), 3D fields otherwise; 8-bit outputs for 4, 8, 6
   switch (conn) {
-    case 26: launch_vcg<T, uint32_t, true>(in, sx, sy, sz, out, 0x3ffffffu, s); break;
-    case 18: launch_vcg<T, uint32_t, true>(in, sx, sy, sz, out, 0x3ffffu, s); break;
-    case 6: launch_vcg<T, uint8_t, true>(in, sx, sy, sz, out, 0x3fu, s); break;
-    case 8: launch_vcg<T, uint8_t, false>(in, sx, sy, sz, out, 0xffu, s); break;
-    default: launch_vcg<T, uint8_t, false>(in, sx, sy, sz, out, 0x0fu, s); break;
+    case 26: launch_vcg<T, uint32_t, true>(in, sx, sy, sz, out, 0x3ffffffu, rev, s); break;
+    case 18: launch_vcg<T, uint32_t, true>(in, sx, sy, sz, out, 0x3ffffu, rev, s); break;
+    case 6: launch_vcg<T, uint8_t, true>(in, sx, sy, sz, out, 0x3fu, rev, s); break;
+    case 8: launch_vcg<T, uint8_t, false>(in, sx, sy, sz, out, 0xffu, rev, s); break;
+    default: launch_vcg<T, uint8_t, false>(in, sx, sy, sz, out, 0x0fu, rev, s); break;
   }
 }
 
 }  // namespace
 
 extern "C" int cc3d_gpu_voxel_connectivity_graph(const void* labels, int label_bytes, int64_t sx, int64_t sy,
-                                                 int64_t sz, int connectivity, void* graph, void* stream) {
+                                                 int64_t sz, int connectivity, int reversed_axes, void* graph,
+                                                 void* stream) {
   if ((label_bytes != 1 && label_bytes != 2 && label_bytes != 4 && label_bytes != 8) || sx < 0 || sy < 0 ||
-      sz < 0)
+      sz < 0 || (reversed_axes != 0 && reversed_axes != 2 && reversed_axes != 3))
     return failf(CC3D_ERR_INVALID, "invalid arguments");
   if (connectivity != 26 && connectivity != 18 && connectivity != 6 && connectivity != 8 && connectivity != 4)
     return failf(CC3D_ERR_RUNTIME, "Only 4 and 8 2D and 6, 18, and 26 3D connectivities are supported.");
+  // (a reversed 2D array has memory extents (sy, sx, 1): still one plane)
   if ((connectivity == 8 || connectivity == 4) && sz != 1)
     return failf(CC3D_ERR_RUNTIME, "sz must be 1 for 2D connectivities.");
   const int64_t voxels = sx * sy * sz;
@@ -129,10 +142,10 @@ extern "C" int cc3d_gpu_voxel_connectivity_graph(const void* labels, int label_b
     return failf(CC3D_ERR_UNSUPPORTED, "volume too large");
   cudaStream_t s = (cudaStream_t)stream;
   switch (label_bytes) {
-    case 1: launch_vcg_t<uint8_t>(labels, sx, sy, sz, connectivity, graph, s); break;
-    case 2: launch_vcg_t<uint16_t>(labels, sx, sy, sz, connectivity, graph, s); break;
-    case 4: launch_vcg_t<uint32_t>(labels, sx, sy, sz, connectivity, graph, s); break;
-    default: launch_vcg_t<uint64_t>(labels, sx, sy, sz, connectivity, graph, s); break;
+    case 1: launch_vcg_t<uint8_t>(labels, sx, sy, sz, connectivity, graph, reversed_axes, s); break;
+    case 2: launch_vcg_t<uint16_t>(labels, sx, sy, sz, connectivity, graph, reversed_axes, s); break;
+    case 4: launch_vcg_t<uint32_t>(labels, sx, sy, sz, connectivity, graph, reversed_axes, s); break;
+    default: launch_vcg_t<uint64_t>(labels, sx, sy, sz, connectivity, graph, reversed_axes, s); break;
   }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -449,14 +449,20 @@ int cc3d_gpu_connected_components3d_noalloc(
  * the same label or lies outside it.  Replaces
  * extract_voxel_connectivity_graph<T,OUT> (cc3d/cc3d_graphs.hpp:31-240,
  * bound at cc3d/fastcc3d.pyx:1021-1178).  `labels` holds sx*sy*sz unsigned
- * integers of label_bytes (1, 2, 4, 8) with x fastest; `graph` receives uint8
- * fields for connectivity 4, 8 and 6 and uint32 fields for 18 and 26 (bit
- * layout of the reference: 2D +x -x +y -y xy -xy x-y -x-y; 3D faces, edges,
- * corners).  4 and 8 need sz == 1.  Synchronises `stream`.
+ * integers of label_bytes (1, 2, 4, 8); sx, sy, sz are the memory extents,
+ * fastest first.  With reversed_axes == 0 memory runs x fastest (the
+ * reference's Fortran order: x is the array's first axis); with 3 (a 3D
+ * array) or 2 (a 2D array) the array is C-ordered, its axes stored in
+ * reverse, so the extents are those of (z, y, x) or (y, x, 1) -- and the
+ * field is still the reference's.
+ * `graph` receives, in the same memory order, uint8 fields for connectivity
+ * 4, 8 and 6 and uint32 fields for 18 and 26 (bit layout of the reference:
+ * 2D +x -x +y -y xy -xy x-y -x-y; 3D faces, edges, corners).  4 and 8 need
+ * sz == 1.  Synchronises `stream`.
  */
 int cc3d_gpu_voxel_connectivity_graph(
     const void* labels, int label_bytes, int64_t sx, int64_t sy, int64_t sz,
-    int connectivity, void* graph, void* stream);
+    int connectivity, int reversed_axes, void* graph, void* stream);
 
 #ifdef __cplusplus
 }
