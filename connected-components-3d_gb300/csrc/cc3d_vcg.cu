@@ -39,60 +39,98 @@ constexpr int BXW = VX + 2, BYW = VY + 2, BZW = VZ + 2;  // staged box with halo
 // REV = 3 (3D arrays) memory offsets (a, b, c) are the field's directions
 // (x, y, z) = (c, b, a); with REV = 2 (2D arrays) (x, y, z) = (b, a, c).
 // sx, sy, sz are the memory extents, fastest first.
+template <int REV, bool D3>
+__device__ __forceinline__ int field_bit(int da, int db, int dc) {
+  if (!D3) return REV ? dir_bit2(db, da) : dir_bit2(da, db);
+  return REV == 3 ? dir_bit3(dc, db, da) : REV == 2 ? dir_bit3(db, da, dc) : dir_bit3(da, db, dc);
+}
+
 template <typename T, typename OUT, bool D3, int REV>
 __global__ void __launch_bounds__(VX * VY) k_vcg(const T* __restrict__ in, int64_t sx, int64_t sy, int64_t sz,
                                                  OUT* __restrict__ out, uint32_t mask, int64_t nbx, int64_t nby) {
-  __shared__ T box[BZW][BYW][BXW];
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * VX + tx;
+  constexpr int NZ = D3 ? BZW : 1;  // staged planes (one for 2D fields)
+  __shared__ T box[NZ][BYW][BXW];
+  const int tx = threadIdx.x, ty = threadIdx.y;
   int64_t b = blockIdx.x;
   const int64_t bx = b % nbx;
   b /= nbx;
   const int64_t by = b % nby, bz = b / nby;
   const int64_t x0 = bx * VX, y0 = by * VY, z0 = bz * VZ;
-  // stage the box (out-of-volume entries are never compared)
-  for (int i = tid; i < BZW * BYW * BXW; i += VX * VY) {
-    const int lx = i % BXW, ly = (i / BXW) % BYW, lz = i / (BXW * BYW);
-    const int64_t gx = x0 - 1 + lx, gy = y0 - 1 + ly, gz = z0 - 1 + lz;
-    T v = T(0);
-    if (gx >= 0 && gx < sx && gy >= 0 && gy < sy && gz >= 0 && gz < sz) v = in[(gz * sy + gy) * sx + gx];
-    box[lz][ly][lx] = v;
+  // stage the box row by row, coalesced along x (out-of-volume entries are
+  // never compared: their directions are set from the coordinates)
+  for (int r = ty; r < NZ * BYW; r += VY) {
+    const int lz = r / BYW, ly = r - lz * BYW;
+    const int64_t gy = y0 - 1 + ly, gz = D3 ? z0 - 1 + lz : 0;
+    const bool rowin = gy >= 0 && gy < sy && gz >= 0 && gz < sz;
+    const T* row = in + (gz * sy + gy) * sx;
+    for (int c = tx; c < BXW; c += VX) {
+      const int64_t gx = x0 - 1 + c;
+      box[lz][ly][c] = (rowin && gx >= 0 && gx < sx) ? row[gx] : T(0);
+    }
   }
   __syncthreads();
   const int64_t x = x0 + tx, y = y0 + ty;
   if (x >= sx || y >= sy) return;
-  // which neighbours exist, per axis and side
   const bool xm = x > 0, xp = x < sx - 1, ym = y > 0, yp = y < sy - 1;
+  // directions whose neighbour lies outside the volume keep their bit
+  uint32_t oob_xy = 0;
+#pragma unroll
+  for (int dc = -1; dc <= 1; ++dc)
+#pragma unroll
+    for (int db = -1; db <= 1; ++db)
+#pragma unroll
+      for (int da = -1; da <= 1; ++da) {
+        if ((!D3 && dc) || (!da && !db && !dc)) continue;
+        const bool out_ab = (da < 0 && !xm) || (da > 0 && !xp) || (db < 0 && !ym) || (db > 0 && !yp);
+        if (out_ab) oob_xy |= 1u << field_bit<REV, D3>(da, db, dc);
+      }
+  if (!D3) {
+    const T cur = box[0][ty + 1][tx + 1];
+    uint32_t bits = oob_xy;
+#pragma unroll
+    for (int db = -1; db <= 1; ++db)
+#pragma unroll
+      for (int da = -1; da <= 1; ++da)
+        if (da || db) bits |= (uint32_t)(box[0][ty + 1 + db][tx + 1 + da] == cur) << field_bit<REV, D3>(da, db, 0);
+    out[y * sx + x] = (OUT)(bits & mask);
+    return;
+  }
+  // slide a 3 x 3 x 3 window of registers along c (memory z)
+  T w[3][3][3];  // [dc + 1][db + 1][da + 1]
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) w[k + 1][j][i] = box[k][ty + j][tx + i];
+  uint32_t up_bits = 0, down_bits = 0;  // the dc = +1 / -1 directions
+#pragma unroll
+  for (int db = -1; db <= 1; ++db)
+#pragma unroll
+    for (int da = -1; da <= 1; ++da) {
+      up_bits |= 1u << field_bit<REV, D3>(da, db, 1);
+      down_bits |= 1u << field_bit<REV, D3>(da, db, -1);
+    }
   for (int lz = 0; lz < VZ; ++lz) {
     const int64_t z = z0 + lz;
     if (z >= sz) break;
-    const bool zm = z > 0, zp = z < sz - 1;
-    const T cur = box[lz + 1][ty + 1][tx + 1];
-    uint32_t bits = 0;
-    if (D3) {
 #pragma unroll
-      for (int dz = -1; dz <= 1; ++dz)
+    for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
+      for (int i = 0; i < 3; ++i) {
+        w[0][j][i] = w[1][j][i];
+        w[1][j][i] = w[2][j][i];
+        w[2][j][i] = box[lz + 2][ty + j][tx + i];
+      }
+    const T cur = w[1][1][1];
+    uint32_t bits = oob_xy | (z > 0 ? 0u : down_bits) | (z < sz - 1 ? 0u : up_bits);
 #pragma unroll
-          for (int dx = -1; dx <= 1; ++dx) {
-            if (!dx && !dy && !dz) continue;
-            const bool exists = (dx < 0 ? xm : (dx > 0 ? xp : true)) && (dy < 0 ? ym : (dy > 0 ? yp : true)) &&
-                                (dz < 0 ? zm : (dz > 0 ? zp : true));
-            const bool differs = exists && box[lz + 1 + dz][ty + 1 + dy][tx + 1 + dx] != cur;
-            if (!differs)
-              bits |= 1u << (REV == 3 ? dir_bit3(dz, dy, dx) : REV == 2 ? dir_bit3(dy, dx, dz) : dir_bit3(dx, dy, dz));
-          }
-    } else {
+    for (int dc = -1; dc <= 1; ++dc)
 #pragma unroll
-      for (int dy = -1; dy <= 1; ++dy)
+      for (int db = -1; db <= 1; ++db)
 #pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-          if (!dx && !dy) continue;
-          const bool exists = (dx < 0 ? xm : (dx > 0 ? xp : true)) && (dy < 0 ? ym : (dy > 0 ? yp : true));
-          const bool differs = exists && box[1][ty + 1 + dy][tx + 1 + dx] != cur;
-          if (!differs) bits |= 1u << (REV ? dir_bit2(dy, dx) : dir_bit2(dx, dy));
-        }
-    }
+        for (int da = -1; da <= 1; ++da)
+          if (da || db || dc) bits |= (uint32_t)(w[dc + 1][db + 1][da + 1] == cur) << field_bit<REV, D3>(da, db, dc);
     out[(z * sy + y) * sx + x] = (OUT)(bits & mask);
   }
 }
