@@ -4,15 +4,17 @@
 //
 //   k_tile_runs   one CTA per 32 x TY x TZ tile of 2048 voxels [65536 CTAs].
 //                 Stages the tile plus a one-voxel backward halo in shared
-//                 memory as rows of 32 values (x-aligned, one warp per row) and
-//                 two halo columns.  Rows are cut into runs of related voxels
-//                 with warp ballots; only run heads take part in the tile's
-//                 union-find, so trees stay shallow.  Every row is matched with
-//                 its backward rows (the connectivity's neighbour rows) using
-//                 three ballots (dx = -1, 0, +1) and one union per pair of
-//                 overlapping runs.  Halo runs/voxels that are connected inside
-//                 their own tile are grouped in a second forest, so that one
-//                 edge per (component, halo group) leaves the tile.  Writes
+//                 memory by one TMA copy (rows of 32 values with the two halo
+//                 columns).  Rows are cut into runs of related voxels with warp
+//                 ballots; only run heads take part in the tile's union-find,
+//                 so trees stay shallow.  Every row is matched with its
+//                 backward rows (the connectivity's neighbour rows) by ballots
+//                 (dx = 0, and dx = -1/+1 where the primary neighbour does not
+//                 decide) and one union per pair of overlapping runs.  One edge
+//                 per halo run joined to a tile component leaves the tile,
+//                 except where the same-owner voxel just before it already
+//                 carries the same join.  (k_tile_scan, the warp-per-tile raster
+//                 scan, produces the same records.)  Writes
 //                   rmask[tile][row]   (foreground mask, run-start mask)
 //                   rrow[tile][row]    first run of the row in rcomp
 //                   rcomp[tile][run]   16-bit local component of every run
