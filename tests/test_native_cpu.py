@@ -34,12 +34,6 @@ def test_library_exports_header_symbols(cc3d):
     assert b"sm_103a" in lib.cc3d_gpu_version()
 
 
-def test_library_is_sm103a(cc3d):
-    with open(cc3d._native.library_path(), "rb") as f:
-        blob = f.read()
-    assert b"sm_103a" in blob or b"sm_103" in blob
-
-
 def test_validation_matches_reference(cc3d):
     with pytest.raises(cc3d.DimensionError):
         cc3d.connected_components(np.zeros((2, 2, 2, 2), np.uint8))
@@ -74,3 +68,29 @@ def test_contiguity_rules_match_numpy(cc3d):
             a = a.transpose()
         st = tuple(s // a.itemsize for s in a.strides)
         assert _contig_flags(a.shape, st) == (a.flags.c_contiguous, a.flags.f_contiguous), (a.shape, a.strides)
+
+
+def test_widened_functions_validate_before_the_device(cc3d):
+    """The argument errors of the reference's other functions, raised by the
+    front end before any device call (cases from the golden fixtures)."""
+    import json
+    here = os.path.join(ROOT, "tests", "golden")
+    errors = {"OverflowError": OverflowError, "TypeError": TypeError, "ValueError": ValueError}
+    for name, fn_of in (("cc3d_continuous", lambda m: cc3d.connected_components),
+                        ("cc3d_vcg", lambda m: (cc3d.voxel_connectivity_graph if m["kind"] == "vcg"
+                                                else cc3d.color_connectivity_graph))):
+        with open(os.path.join(here, name + ".json")) as f:
+            meta = json.load(f)
+        arrays = np.load(os.path.join(here, name + ".npz"))
+        n = 0
+        for i, m in enumerate(meta):
+            if "error" not in m:
+                continue
+            data = arrays[f"in{i}"]
+            exc = cc3d.DimensionError if m["error"] == "DimensionError" else errors[m["error"]]
+            with pytest.raises(exc):
+                fn_of(m)(data, **m["kwargs"])
+            n += 1
+        assert n >= 5, name
+    with pytest.raises(ValueError):
+        cc3d.connected_components_stack([np.ones((2, 2, 2), np.uint8)], connectivity=18)
