@@ -334,7 +334,7 @@ def run_gpu(args, world, rank, local):
     # persistent host threads: the library keeps one device workspace per
     # thread, so the same threads serve the warm-up and the timed steps
     pool = concurrent.futures.ThreadPoolExecutor(E2E_THREADS)
-    gate = threading.Barrier(E2E_THREADS)
+    gate = threading.Barrier(E2E_THREADS, timeout=120)  # a thread that fails cannot hang the others
 
     def e2e_run(nsteps, nthreads):
         # nthreads > 1: volumes alternate between the pool's threads; each
