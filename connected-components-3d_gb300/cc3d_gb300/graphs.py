@@ -262,10 +262,11 @@ def voxel_connectivity_graph(data: Any, connectivity: int = 26):
             flat.data_ptr(), width, sx, sy, sz, int(connectivity), dims if rev else 0, out.data_ptr(),
             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     if rev:
-        if is_t:
-            return out.view(*shape)
-        return np.asfortranarray(out.cpu().numpy().reshape(shape))
-    return _from_f_order(out, shape, is_t)
+        res = out.view(*shape) if is_t else np.asfortranarray(out.cpu().numpy().reshape(shape))
+    else:
+        res = _from_f_order(out, shape, is_t)
+    # CPU tensors in, CPU tensors out (as connected_components does)
+    return res.cpu() if is_t and not data.is_cuda else res
 
 
 def color_connectivity_graph(vcg: Any, connectivity: int = 26, return_N: bool = False):
@@ -313,5 +314,7 @@ def color_connectivity_graph(vcg: Any, connectivity: int = 26, return_N: bool = 
         nat.check(lib.cc3d_gpu_label_finish(info.token, n, out.data_ptr(), nat.U32, ctypes.byref(cnt),
                                             nat.OUT_DEVICE, stream))
     labels = _from_f_order(out, tuple(shape), is_t)
+    if is_t and not vcg.is_cuda:
+        labels = labels.cpu()
     N = int(cnt.value)
     return (labels, N) if return_N else labels
