@@ -178,6 +178,14 @@ def profile_read() -> dict:
     return {name: (ms[i], int(cnt[i])) for i, name in enumerate(PROFILE_STAGES)}
 
 
+def dev_ptr(t) -> int:
+    """The device address of a CUDA tensor; anything else is refused here, so
+    that no host address ever reaches a kernel."""
+    if not getattr(t, "is_cuda", False):
+        raise RuntimeError("internal error: a device buffer was expected (got a host tensor)")
+    return t.data_ptr()
+
+
 def check(rc: int) -> None:
     """Raise the Python exception the reference raises for this failure."""
     if rc == OK:

@@ -122,7 +122,7 @@ class _Dev:
         return _contig_flags(self.t.shape, self.t.stride())
 
     def ptr(self):
-        return self.t.data_ptr()
+        return nat.dev_ptr(self.t)
 
     def stream(self):
         return ctypes.c_void_p(_torch().cuda.current_stream(self.t.device).cuda_stream)
@@ -166,7 +166,7 @@ def estimate_provisional_labels(data) -> Tuple[int, int, int]:
             c, f = True, False
         sx = t.shape[0] if f else t.shape[-1]
         with _torch().cuda.device(t.device):
-            return _epl_call(t.data_ptr(), _CODE[d.npdtype], sx, t.numel(), nat.IN_DEVICE, d.stream())
+            return _epl_call(nat.dev_ptr(t), _CODE[d.npdtype], sx, t.numel(), nat.IN_DEVICE, d.stream())
     if _is_torch(data):
         data = data.cpu().numpy()
     if data.dtype not in _CODE:
@@ -299,7 +299,7 @@ def connected_components(
         stream = dev.stream()
         torch = _torch()
         devctx = torch.cuda.device(t.device)
-        ptr = t.data_ptr()
+        ptr = nat.dev_ptr(t)
     else:
         stream = None
         devctx = None
@@ -377,7 +377,7 @@ def connected_components(
     elif on_device:
         maker = torch.zeros if special else torch.empty
         out = maker((voxels,), dtype=_torch_dtype(out_dtype), device=t.device)
-        out_ptr, mem_out = out.data_ptr(), nat.OUT_DEVICE
+        out_ptr, mem_out = nat.dev_ptr(out), nat.OUT_DEVICE
     else:
         out = np.zeros((voxels,), dtype=out_dtype, order="F")
         out_ptr, mem_out = out.ctypes.data, 0
@@ -465,7 +465,7 @@ def statistics(out_labels: Any, no_slice_conversion: bool = False) -> dict:
             t = t.contiguous()
             c, f = True, False
         c_order = 0 if (f and not c) else 1
-        ptr, mem = t.data_ptr(), nat.IN_DEVICE | nat.OUT_DEVICE
+        ptr, mem = nat.dev_ptr(t), nat.IN_DEVICE | nat.OUT_DEVICE
         stream = ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
         devctx = torch.cuda.device(t.device)
     else:
@@ -511,7 +511,7 @@ def statistics(out_labels: Any, no_slice_conversion: bool = False) -> dict:
         counts = torch.empty((N + 1,), dtype=_torch_dtype(np.uint32), device=t.device)
         bboxes = torch.empty((N + 1, 2 * ndim), dtype=_torch_dtype(bdt), device=t.device)
         cents = torch.empty((N + 1, ndim), dtype=torch.float64, device=t.device)
-        pc, pb, pcen = counts.data_ptr(), bboxes.data_ptr(), cents.data_ptr()
+        pc, pb, pcen = nat.dev_ptr(counts), nat.dev_ptr(bboxes), nat.dev_ptr(cents)
     else:
         counts = np.zeros(N + 1, dtype=np.uint32)
         bboxes = np.zeros((N + 1, 2 * ndim), dtype=bdt)

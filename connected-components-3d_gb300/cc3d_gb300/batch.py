@@ -75,8 +75,8 @@ def _descriptors(volumes):
     pool = torch.empty((int(sizes.sum()),), dtype=torch.uint8, device=devs[0].device)
     offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
     vols = np.empty(n, _VOLUME_DTYPE)
-    vols["in"] = [d.data_ptr() for d in devs]
-    vols["out"] = pool.data_ptr() + offs
+    vols["in"] = [nat.dev_ptr(d) for d in devs]
+    vols["out"] = nat.dev_ptr(pool) + offs
     vols["sx"], vols["sy"], vols["sz"] = shapes[:, 2], shapes[:, 1], shapes[:, 0]
     res = np.zeros(n, _RESULT_DTYPE)
     outs = pool.split([int(v) for v in sizes])

@@ -47,7 +47,9 @@ def _flat_device(x):
     torch = _torch()
     if _is_torch(x):
         t = x.contiguous().view(-1)
-        return t.view(torch.uint8) if t.dtype != torch.bool else t.view(torch.uint8)
+        if not t.is_cuda:
+            t = t.cuda()
+        return t.view(torch.uint8)
     a = np.ascontiguousarray(np.asarray(x)).reshape(-1)
     return torch.from_numpy(a.view(np.uint8)).cuda()
 
@@ -130,14 +132,12 @@ def _zero_labels(img, cc_labels, zero: np.ndarray) -> None:
     lab_bytes = cc_labels.element_size() if _is_torch(cc_labels) else cc_labels.dtype.itemsize
     img_bytes = img.element_size() if _is_torch(img) else img.dtype.itemsize
     n = img.numel() if _is_torch(img) else img.size
-    if _is_torch(img) and img.is_contiguous():
-        target = img.view(-1).view(torch.uint8)
-    else:
-        target = _flat_device(img)
-    nat.check(lib.cc3d_gpu_zero_labels(target.data_ptr(), img_bytes, lab.data_ptr(), lab_bytes, n,
-                                       ztab.data_ptr(), zero.size, _stream()))
+    in_place = _is_torch(img) and img.is_cuda and img.is_contiguous()
+    target = img.view(-1).view(torch.uint8) if in_place else _flat_device(img)
+    nat.check(lib.cc3d_gpu_zero_labels(nat.dev_ptr(target), img_bytes, nat.dev_ptr(lab), lab_bytes, n,
+                                       nat.dev_ptr(ztab), zero.size, _stream()))
     if _is_torch(img):
-        if not img.is_contiguous():
+        if not in_place:
             img.copy_(target.view(img.dtype).view(img.shape))
         return
     img[...] = target.cpu().numpy().view(img.dtype).reshape(img.shape)
@@ -154,13 +154,15 @@ def _remap(cc_labels, table: np.ndarray, out_dtype, order: str = "C"):
     otab = torch.from_numpy(table.view(np.uint8)).cuda()
     width = table.dtype.itemsize
     out = torch.empty((max(1, n) * width,), dtype=torch.uint8, device=lab.device)
-    nat.check(lib.cc3d_gpu_remap_labels(lab.data_ptr(), lab_bytes, n, otab.data_ptr(), width, table.size,
-                                        out.data_ptr(), _stream()))
+    nat.check(lib.cc3d_gpu_remap_labels(nat.dev_ptr(lab), lab_bytes, n, nat.dev_ptr(otab), width, table.size,
+                                        nat.dev_ptr(out), _stream()))
     out = out[:n * width]
     if _is_torch(cc_labels):
         if out_dtype == np.bool_:
-            return out.view(torch.bool).view(cc_labels.shape)
-        return out.view(getattr(torch, np.dtype(out_dtype).name)).view(cc_labels.shape)
+            res = out.view(torch.bool).view(cc_labels.shape)
+        else:
+            res = out.view(getattr(torch, np.dtype(out_dtype).name)).view(cc_labels.shape)
+        return res if cc_labels.is_cuda else res.cpu()
     host = out.cpu().numpy().view(np.bool_ if out_dtype == np.bool_ else out_dtype).reshape(cc_labels.shape)
     return np.asfortranarray(host) if order == "F" else host
 

@@ -28,6 +28,8 @@ def contacts(labels: Any, connectivity: int = 26, surface_area: bool = True,
         while t.dim() < 3:
             t = t.unsqueeze(-1)
         dev = t.permute(*reversed(range(t.dim()))).contiguous()  # x fastest in memory
+        if not dev.is_cuda:
+            dev = dev.cuda()
         sx, sy, sz = (int(v) for v in t.shape)
         width = t.element_size()
         if t.is_floating_point():
@@ -50,7 +52,7 @@ def contacts(labels: Any, connectivity: int = 26, surface_area: bool = True,
     n = ctypes.c_uint64(0)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     with torch.cuda.device(dev.device):
-        nat.check(lib.cc3d_gpu_contacts(dev.data_ptr(), width, sx, sy, sz, int(connectivity), ctypes.byref(n),
+        nat.check(lib.cc3d_gpu_contacts(nat.dev_ptr(dev), width, sx, sy, sz, int(connectivity), ctypes.byref(n),
                                         stream))
     npairs = int(n.value)
     if npairs == 0:
@@ -84,6 +86,8 @@ def _flat_memory_order(labels):
         t = labels
         if not t.is_contiguous():
             t = t.permute(*reversed(range(t.dim()))).contiguous()
+        if not t.is_cuda:
+            t = t.cuda()
         return t.reshape(-1).view(torch.uint8), t.element_size(), t.numel()
     a = np.asarray(labels)
     flat = a.reshape(-1, order="F" if a.flags.f_contiguous and not a.flags.c_contiguous else "C")
@@ -105,7 +109,7 @@ def runs(labels: Any) -> Dict[int, list]:
     lib = nat.load()
     cnt = ctypes.c_uint64(0)
     with torch.cuda.device(dev.device):
-        nat.check(lib.cc3d_gpu_run_starts(dev.data_ptr(), width, n, ctypes.byref(cnt),
+        nat.check(lib.cc3d_gpu_run_starts(nat.dev_ptr(dev), width, n, ctypes.byref(cnt),
                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     m = int(cnt.value)
     pos = np.empty(m, np.uint64)
@@ -259,7 +263,7 @@ def voxel_connectivity_graph(data: Any, connectivity: int = 26):
     lib = nat.load()
     with torch.cuda.device(flat.device):
         nat.check(lib.cc3d_gpu_voxel_connectivity_graph(
-            flat.data_ptr(), width, sx, sy, sz, int(connectivity), dims if rev else 0, out.data_ptr(),
+            nat.dev_ptr(flat), width, sx, sy, sz, int(connectivity), dims if rev else 0, nat.dev_ptr(out),
             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     if rev:
         res = out.view(*shape) if is_t else np.asfortranarray(out.cpu().numpy().reshape(shape))
@@ -308,10 +312,10 @@ def color_connectivity_graph(vcg: Any, connectivity: int = 26, return_N: bool = 
     with torch.cuda.device(flat.device):
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         info = nat.Prepared()
-        nat.check(lib.cc3d_gpu_label_prepare_graph(flat.data_ptr(), nat.U8 if npd == np.uint8 else nat.U32,
+        nat.check(lib.cc3d_gpu_label_prepare_graph(nat.dev_ptr(flat), nat.U8 if npd == np.uint8 else nat.U32,
                                                    sx, sy, sz, int(connectivity),
                                                    nat.IN_DEVICE | nat.OUT_DEVICE, stream, ctypes.byref(info)))
-        nat.check(lib.cc3d_gpu_label_finish(info.token, n, out.data_ptr(), nat.U32, ctypes.byref(cnt),
+        nat.check(lib.cc3d_gpu_label_finish(info.token, n, nat.dev_ptr(out), nat.U32, ctypes.byref(cnt),
                                             nat.OUT_DEVICE, stream))
     labels = _from_f_order(out, tuple(shape), is_t)
     if is_t and not vcg.is_cuda:

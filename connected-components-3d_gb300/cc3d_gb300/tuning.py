@@ -73,7 +73,7 @@ def _volume(data: Any):
                np.dtype(np.int32): np.dtype(np.uint32), np.dtype(np.int64): np.dtype(np.uint64),
                np.dtype(np.bool_): np.dtype(np.uint8)}.get(npd, npd)
         shape = list(t.shape)
-        ptr, mem = t.data_ptr(), nat.IN_DEVICE
+        ptr, mem = nat.dev_ptr(t), nat.IN_DEVICE
         stream = ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
         keep = t
     else:
