@@ -133,7 +133,12 @@ static int label_batch(const cc3d_gpu_volume* vols, int n, int dtype, int64_t co
   int64_t vx_sum = 0, vx_n = 0;
   for (int i = 0; i < n; ++i) {
     const int64_t vx = vols[i].sx * vols[i].sy * vols[i].sz;
-    if (vx > 0) { vx_sum += vx; ++vx_n; }
+    if (vx > 0) {
+      if (!device_accessible(vols[i].in) || !device_accessible(vols[i].out))
+        return failf(CC3D_ERR_INVALID, "volume %d: input and output must be device memory", i);
+      vx_sum += vx;
+      ++vx_n;
+    }
   }
   const int code = forced_variant != CC3D_TILE_AUTO ? forced_variant
                                                     : tile_pass_for(dtype, conn, mode, vx_n ? vx_sum / vx_n : 0);

@@ -426,6 +426,8 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
     return fail(CC3D_ERR_INVALID, "periodic_boundary is only implemented for 4, 8 and 6 connectivity");
   if (continuous && (periodic_boundary || binary_image))
     return fail(CC3D_ERR_RUNTIME, "periodic_boundary is not currently supported for continuous data.");
+  if ((mem_flags & CC3D_IN_DEVICE) && sx * sy * sz > 0 && !device_accessible(in))
+    return fail(CC3D_ERR_INVALID, "the input must be device memory with CC3D_IN_DEVICE");
   memset(info, 0, sizeof(*info));
   info->first_row = -1;
   info->last_row = -1;
@@ -619,6 +621,8 @@ int cc3d_gpu_label_finish(uint64_t token, int64_t max_labels, void* out, int out
   *N = 0;
   if (job.empty) return CC3D_OK;
   if (!job.ready) return fail(CC3D_ERR_INVALID, "the prepared labelling did not complete");
+  if ((mem_flags & CC3D_OUT_DEVICE) && !device_accessible(out))
+    return fail(CC3D_ERR_INVALID, "the output must be device memory with CC3D_OUT_DEVICE");
   const size_t osz = dtype_size(out_dtype);
   const int64_t voxels = job.voxels;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);
@@ -819,6 +823,11 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   if (bbox_dtype != CC3D_U16 && bbox_dtype != CC3D_U32) return fail(CC3D_ERR_INVALID, "bbox dtype");
   const int64_t voxels = d0 * d1 * d2;
   if (N > (uint64_t)voxels) return fail(CC3D_ERR_INVALID, "N exceeds the voxel count");
+  if ((mem_flags & CC3D_IN_DEVICE) && !device_accessible(labels))
+    return fail(CC3D_ERR_INVALID, "labels must be device memory with CC3D_IN_DEVICE");
+  if ((mem_flags & CC3D_OUT_DEVICE) &&
+      !(device_accessible(counts) && device_accessible(bboxes) && device_accessible(centroids)))
+    return fail(CC3D_ERR_INVALID, "outputs must be device memory with CC3D_OUT_DEVICE");
   Workspace* w;
   if (int rc = get_ws_fresh(w)) return rc;
   cudaStream_t s = pick_stream(*w, stream, mem_flags);

@@ -214,7 +214,7 @@ extern "C" int cc3d_gpu_contacts(const void* labels, int label_bytes, int64_t sx
   g_contacts.n = 0;
   const int64_t voxels = sx * sy * sz;
   if (voxels == 0) return CC3D_OK;
-  if (!labels) return failf(CC3D_ERR_INVALID, "invalid arguments");
+  if (!device_accessible(labels)) return failf(CC3D_ERR_INVALID, "labels must be device memory");
   cudaStream_t s = (cudaStream_t)stream;
   ContactState& st = g_contacts;
   // pass 1: an upper bound on the pairs (warp-merged insert attempts)

@@ -278,12 +278,20 @@ extern "C" int cc3d_gpu_volume_features(const void* in, int dtype, int64_t sx, i
                                         int64_t connectivity, int binary_image, int mem_flags, void* stream,
                                         float* features) {
   if (!features || sx <= 0 || sy <= 0 || sz <= 0) return failf(CC3D_ERR_INVALID, "invalid arguments");
-  if (!(mem_flags & CC3D_IN_DEVICE)) return failf(CC3D_ERR_INVALID, "features need a device volume");
+  if (!(mem_flags & CC3D_IN_DEVICE) || !device_accessible(in))
+    return failf(CC3D_ERR_INVALID, "features need a device volume");
   cudaStream_t s = (cudaStream_t)stream;
-  // one small allocation-free scratch: sums, samples, distinct count
+  // one small scratch per host thread and device: sums, samples, distinct count
   static thread_local void* scratch = nullptr;
+  static thread_local int scratch_dev = -1;
   const size_t bytes = sizeof(FeatureSums) + kDistinct * sizeof(unsigned long long) + 16;
-  if (!scratch) CKC(cudaMalloc(&scratch, bytes));
+  int dev = 0;
+  CKC(cudaGetDevice(&dev));
+  if (scratch && scratch_dev != dev) scratch = nullptr;  // kept for the other device's lifetime
+  if (!scratch) {
+    CKC(cudaMalloc(&scratch, bytes));
+    scratch_dev = dev;
+  }
   FeatureSums* sums = (FeatureSums*)scratch;
   unsigned long long* samples = (unsigned long long*)((char*)scratch + sizeof(FeatureSums));
   unsigned int* dcount = (unsigned int*)(samples + kDistinct);

@@ -118,6 +118,8 @@ extern "C" int cc3d_gpu_remap_labels(const void* labels, int label_bytes, int64_
       !table || table_len == 0)
     return failf(CC3D_ERR_INVALID, "invalid arguments");
   if (voxels == 0) return CC3D_OK;
+  if (!device_accessible(labels) || !device_accessible(table) || !device_accessible(out))
+    return failf(CC3D_ERR_INVALID, "labels, table and output must be device memory");
   cudaStream_t s = (cudaStream_t)stream;
   unsigned* bad;
   if (int rc = bad_flag(&bad)) return rc;
@@ -145,6 +147,8 @@ extern "C" int cc3d_gpu_zero_labels(void* image, int image_bytes, const void* la
       !zero || table_len == 0)
     return failf(CC3D_ERR_INVALID, "invalid arguments");
   if (voxels == 0) return CC3D_OK;
+  if (!device_accessible(image) || !device_accessible(labels) || !device_accessible(zero))
+    return failf(CC3D_ERR_INVALID, "image, labels and table must be device memory");
   cudaStream_t s = (cudaStream_t)stream;
   unsigned* bad;
   if (int rc = bad_flag(&bad)) return rc;

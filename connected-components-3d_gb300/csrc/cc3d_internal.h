@@ -75,6 +75,19 @@ void record_tile_pass(int dtype, int eff_connectivity, int mode, int64_t voxels,
 
 // set the calling thread's error message (returns code); map a device error
 // word to a return code (cc3d_capi.cu)
+// True if a kernel of this device may dereference p: device or managed
+// memory.  Host addresses (pinned or not) are refused, so that a wrong
+// argument returns an error instead of faulting the device.
+inline bool device_accessible(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
 int api_fail(int code, const char* msg);
 int api_device_errors(unsigned err);
 

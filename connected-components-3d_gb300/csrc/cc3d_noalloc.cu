@@ -125,7 +125,8 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   if (__builtin_mul_overflow(sx, sy, &voxels) || __builtin_mul_overflow(voxels, sz, &voxels))
     return failf(CC3D_ERR_INVALID, "volume size overflows int64");
   if (voxels == 0) return CC3D_OK;
-  if (!in || !out) return failf(CC3D_ERR_INVALID, "invalid arguments");
+  if (!device_accessible(in) || !device_accessible(out))
+    return failf(CC3D_ERR_INVALID, "input and output must be device memory");
   // every voxel takes more than one byte of scratch: larger volumes cannot fit
   if (voxels > (int64_t)CC3D_NOALLOC_SCRATCH_BYTES)
     return failf(CC3D_ERR_INVALID,

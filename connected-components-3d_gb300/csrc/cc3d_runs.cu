@@ -170,6 +170,7 @@ extern "C" int cc3d_gpu_run_starts(const void* labels, int label_bytes, int64_t 
   *nstarts = 0;
   g_runs.n = 0;
   if (voxels == 0) return CC3D_OK;
+  if (!device_accessible(labels)) return failf(CC3D_ERR_INVALID, "labels must be device memory");
   cudaStream_t s = (cudaStream_t)stream;
   int rc;
   switch (label_bytes) {

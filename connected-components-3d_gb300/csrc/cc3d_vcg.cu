@@ -175,7 +175,8 @@ extern "C" int cc3d_gpu_voxel_connectivity_graph(const void* labels, int label_b
     return failf(CC3D_ERR_RUNTIME, "sz must be 1 for 2D connectivities.");
   const int64_t voxels = sx * sy * sz;
   if (voxels == 0) return CC3D_OK;
-  if (!labels || !graph) return failf(CC3D_ERR_INVALID, "invalid arguments");
+  if (!device_accessible(labels) || !device_accessible(graph))
+    return failf(CC3D_ERR_INVALID, "labels and graph must be device memory");
   if ((sx + VX - 1) / VX * ((sy + VY - 1) / VY) * ((sz + VZ - 1) / VZ) >= (1ll << 31))
     return failf(CC3D_ERR_UNSUPPORTED, "volume too large");
   cudaStream_t s = (cudaStream_t)stream;
