@@ -622,7 +622,7 @@ def run_costmodel(args):
     """Train the cost model on autotuner timings of `args.costmodel` generated
     volumes (Voronoi with 1 to ~1e6 seeds, Bernoulli p 0.05-0.95, multilabel
     Bernoulli K 2-1000; uint8/16/32/64; edges 64-320; connectivity 26/18/6)
-    and judge it on a held-out-seed stream by its regret against the
+    and evaluate it on a held-out-seed stream by its regret against the
     exhaustive autotuner.  One JSON line; the parameters are saved where
     --save-params says (and loaded by set_tile_pass("model") when shipped in
     the package)."""
@@ -670,7 +670,7 @@ def main():
     ap.add_argument("--graphs", action="store_true",
                     help="voxel and colour connectivity graphs of the headline volume instead of the headline")
     ap.add_argument("--costmodel", type=int, default=0,
-                    help="train and judge the cost model on this many generated volumes instead of the headline")
+                    help="train and evaluate the cost model on this many generated volumes instead of the headline")
     ap.add_argument("--save-params", default="", help="where --costmodel saves the trained parameters")
     ap.add_argument("--tile-pass", default="auto",
                     help="tile-pass configuration of the headline run: auto, runs, scan or "
