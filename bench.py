@@ -18,7 +18,7 @@ write of the uint32 output.  Inputs are synthetic and seeded.
            alternate volumes (the library keeps a workspace and stream per
            thread), so one volume's copy-out overlaps the next one's copy-in
            and tile pass; the single-thread figure is reported beside it.
-           Median of three K-step runs, every run listed.
+           Median of five K-step runs, every run listed.
 --impl reference
     The reference's CPU implementation of the path on this machine's host
     cores: the compiled reference where it was built here (oracle/_ref), else
@@ -255,7 +255,7 @@ def run_reference(args, world, rank):
 
 
 E2E_THREADS = 2  # host threads of the end-to-end leg
-E2E_REPS = 3     # timed K-step runs of the end-to-end leg (median reported)
+E2E_REPS = 5     # timed K-step runs of the end-to-end leg (median reported)
 
 
 def run_gpu(args, world, rank, local):

@@ -293,7 +293,7 @@ __device__ __forceinline__ unsigned short sfind(volatile unsigned short* par, un
 
 // find without path compression: used once the unions are done, when every
 // thread only reads the forest (no write may race with the flattening)
-static __device__ __noinline__ unsigned short sfind_ro(const volatile unsigned short* par, unsigned short n) {
+static __device__ __forceinline__ unsigned short sfind_ro(const volatile unsigned short* par, unsigned short n) {
   for (int it = 0; it < kLocalLimit; ++it) {
     const unsigned short p = par[n];
     if (p == n) return n;
@@ -302,9 +302,9 @@ static __device__ __noinline__ unsigned short sfind_ro(const volatile unsigned s
   return n;
 }
 
-// Not inlined: the tile kernel calls it from many sites, and one shared copy
-// keeps the kernel's code inside the instruction cache.
-static __device__ __noinline__ bool sunite(unsigned short* par, unsigned short a, unsigned short b) {
+// Inlined into its one call site in the block-parallel pass (the union
+// runner); callers with many sites use sunite_outlined.
+static __device__ __forceinline__ bool sunite(unsigned short* par, unsigned short a, unsigned short b) {
   volatile unsigned short* vp = par;
   for (int it = 0; it < kLocalLimit; ++it) {
     a = sfind(vp, a);
@@ -315,6 +315,12 @@ static __device__ __noinline__ bool sunite(unsigned short* par, unsigned short a
     if (atomicCAS(par + a, a, b) == a) return true;
   }
   return false;
+}
+
+// One shared copy of sunite for kernels that call it from many sites, which
+// keeps their code inside the instruction cache.
+static __device__ __noinline__ bool sunite_outlined(unsigned short* par, unsigned short a, unsigned short b) {
+  return sunite(par, a, b);
 }
 
 // ------------------------------------------------------ global union-find

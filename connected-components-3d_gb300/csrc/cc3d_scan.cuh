@@ -244,7 +244,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
           for (int k = 0; k < NRN; ++k) {
             if (grp[k] && rel<MODE>(cv, vn[k][ci])) {
               const uint32_t l = ln[k][ci];
-              if (l != kNoLabel && l != lo && !sunite(sm.par, (uint16_t)lo, (uint16_t)l)) err |= ERR_LOCAL_BUDGET;
+              if (l != kNoLabel && l != lo && !sunite_outlined(sm.par, (uint16_t)lo, (uint16_t)l)) err |= ERR_LOCAL_BUDGET;
             }
           }
         }
@@ -344,7 +344,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         if (differs) {
 #pragma unroll
           for (int j = 0; j < NC; ++j)
-            if (cand[j] != kNoLabel && cand[j] != lo && !sunite(sm.par, (uint16_t)lo, cand[j]))
+            if (cand[j] != kNoLabel && cand[j] != lo && !sunite_outlined(sm.par, (uint16_t)lo, cand[j]))
               err |= ERR_LOCAL_BUDGET;
         }
         __syncwarp();
@@ -384,7 +384,7 @@ k_tile_scan(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       // lanes whose root is not the run's join it (rare)
       const bool needmerge = fg && c1 != kNoLabel && c1 != RL;
       if (__any_sync(FULL, needmerge)) {
-        if (needmerge && !sunite(sm.par, RL, (uint16_t)c1)) err |= ERR_LOCAL_BUDGET;
+        if (needmerge && !sunite_outlined(sm.par, RL, (uint16_t)c1)) err |= ERR_LOCAL_BUDGET;
       }
       lc[lane + 1] = fg ? RL : kNoLabel;
       if (lane == 0) sm.fmr[ls] = F;
