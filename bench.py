@@ -16,7 +16,9 @@ write of the uint32 output.  Inputs are synthetic and seeded.
            host->device copy of the input and the device->host copy of the
            labels are inside the timed region.  Two host threads take
            alternate volumes (the library keeps a workspace and stream per
-           thread), so one volume's copy-out overlaps the next one's copy-in
+           thread); each of a volume's two stages (copy-in + tile pass,
+           then numbering + write + copy-out) is held by one thread at a
+           time, so one volume's copy-out overlaps the next one's copy-in
            and tile pass; the single-thread figure is reported beside it.
            Median of five K-step runs, every run listed.
 --impl reference
@@ -32,6 +34,7 @@ from __future__ import annotations
 
 import argparse
 import concurrent.futures
+import contextlib
 import ctypes
 import json
 import os
@@ -320,15 +323,26 @@ def run_gpu(args, world, rank, local):
     ocode = {2: nat.U16, 4: nat.U32, 8: nat.U64}[osz]
     pin_outs = [torch.empty(voxels * osz, dtype=torch.uint8).pin_memory() for _ in range(E2E_THREADS)]
 
-    def e2e_step(pin_out):
+    # With several threads, each of the two stages of a volume is held by one
+    # thread at a time: the copy-in stage (prepare: input copy overlapped with
+    # the tile pass) and the copy-out stage (finish: merge, numbering, write
+    # overlapped with the label copy).  The threads then stay one stage apart,
+    # so a volume's copy-out always runs beside the next volume's copy-in
+    # (opposite directions of the host link) instead of the threads falling
+    # into step and contending for the same direction.
+    stage_in, stage_out = threading.Lock(), threading.Lock()
+
+    def e2e_step(pin_out, staged=False):
         # prepare (input staged once; the estimate comes from the same pass),
         # then write the labels into the pinned host buffer
         info = nat.Prepared()
-        nat.check(lib.cc3d_gpu_label_prepare(host_in.ctypes.data, nat.U32, sx, sy, sz, CONN, 0, 0, 0,
-                                             None, ctypes.byref(info)))
+        with (stage_in if staged else contextlib.nullcontext()):
+            nat.check(lib.cc3d_gpu_label_prepare(host_in.ctypes.data, nat.U32, sx, sy, sz, CONN, 0, 0, 0,
+                                                 None, ctypes.byref(info)))
         n = ctypes.c_uint64(0)
-        nat.check(lib.cc3d_gpu_label_finish(info.token, int(min(info.epl, voxels)), pin_out.data_ptr(),
-                                            ocode, ctypes.byref(n), 0, None))
+        with (stage_out if staged else contextlib.nullcontext()):
+            nat.check(lib.cc3d_gpu_label_finish(info.token, int(min(info.epl, voxels)), pin_out.data_ptr(),
+                                                ocode, ctypes.byref(n), 0, None))
         return n.value
 
     # persistent host threads: the library keeps one device workspace per
@@ -344,7 +358,7 @@ def run_gpu(args, world, rank, local):
         def worker(t):
             torch.cuda.set_device(local)
             gate.wait()  # every pool thread takes one share
-            return [e2e_step(pin_outs[t]) for _ in range(t, nsteps, nthreads)]
+            return [e2e_step(pin_outs[t], staged=True) for _ in range(t, nsteps, nthreads)]
         t0 = time.perf_counter()
         if nthreads == 1:
             ns = [e2e_step(pin_outs[0]) for _ in range(nsteps)]
@@ -425,7 +439,8 @@ def run_gpu(args, world, rank, local):
                 "h2d_bytes_per_step": voxels * isz, "d2h_bytes_per_step": voxels * osz_b,
                 "path": f"C ABI (cc3d_gpu_label_prepare + cc3d_gpu_label_finish) per volume, pinned host "
                         f"buffers, {E2E_THREADS} host threads taking alternate volumes (each with its own "
-                        "workspace and stream, so one volume's label copy-out overlaps the next one's "
+                        "workspace and stream; the prepare stage and the finish stage are each held by one "
+                        "thread at a time, so one volume's label copy-out overlaps the next one's "
                         "copy-in and tile pass); within a call input and labels cross in 8 chunks "
                         "overlapped with the tile pass and the writer",
                 "repetitions": {"runs": E2E_REPS, "steps_each": args.steps,
