@@ -563,15 +563,119 @@ def run_graphs(args):
                       "steps": args.steps, "warmup": args.warmup, "N": int(res[1])}), flush=True)
 
 
+# ------------------------------------------------------------ statistics
+def run_statistics(args):
+    """Device-resident statistics (voxel counts, bounding boxes, centroids; no
+    slice conversion) of the labels of the headline volume, one JSON line.
+    Algorithmic bytes: one read of the labels plus the three tables,
+    sizeof(label) * voxels + (N + 1) * (4 + 6 * sizeof(bbox) + 24).  The
+    result is checked against the oracle's, which is timed beside it on one
+    host core."""
+    import torch
+    import cc3d_gb300 as cc3d
+    cc3d.build()
+    peak, peak_kind = load_peaks()
+    vol = make_volume(0)
+    labels, N = cc3d.connected_components(torch.from_numpy(vol).cuda(), connectivity=CONN, return_N=True)
+    voxels = labels.numel()
+
+    def stats():
+        return cc3d.statistics(labels, no_slice_conversion=True)
+
+    for _ in range(args.warmup):
+        stats()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        got = stats()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    bbox_bytes = got["bounding_boxes"].element_size()
+    nbytes = voxels * labels.element_size() + (N + 1) * (4 + 6 * bbox_bytes + 24)
+    host = labels.cpu().numpy()
+    import oracle
+    times, t_start = [], time.perf_counter()
+    while len(times) < 3 and time.perf_counter() - t_start < 20.0:
+        t0 = time.perf_counter()
+        exp = oracle.statistics(host, no_slice_conversion=True)
+        times.append(time.perf_counter() - t0)
+    exact = all(np.array_equal(got[k].cpu().numpy(), exp[k], equal_nan=(k == "centroids"))
+                for k in ("voxel_counts", "bounding_boxes", "centroids"))
+    assert exact, "statistics differ from the oracle"
+    best = min(times)
+    print(json.dumps({
+        "metric": "GVoxels/s statistics of the 512^3 uint32 labels (counts, boxes, centroids; exact)",
+        "value": voxels / ms / 1e6, "unit": "GVoxels/s", "ms_per_step": ms, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "N": int(N), "exact_vs_oracle": exact,
+        "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak, "unit": "GB/s",
+                     "frac": nbytes / ms / 1e6 / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_step": nbytes},
+        "cpu_baseline": {"value": voxels / best / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": "port",
+                         "sample": f"the same labels, oracle's numpy restatement, best of {len(times)} "
+                                   f"({best:.3f} s)"},
+        "config": {"workload": "labels of the 512^3 uint32 Voronoi volume at connectivity 26 "
+                               "(device tensors in and out)", "l2": "labels (512 MiB) larger than L2"},
+    }), flush=True)
+
+
 # ------------------------------------------------------------ batched stream
+_STREAM = None
+
+
+def _stream_worker_init(path: str) -> None:
+    global _STREAM
+    _STREAM = np.load(path, mmap_mode="r")
+
+
+def _stream_worker_label(task):
+    """One volume of the mixed-size stream by the reference's CPU path (the
+    compiled reference where present, else the oracle port); returns voxels."""
+    import oracle
+    off, shape, kind = task
+    n = int(np.prod(shape))
+    vol = np.ascontiguousarray(_STREAM[off:off + n]).reshape(shape)
+    oracle.connected_components(vol, connectivity=26, backend=kind)
+    return n
+
+
+def cpu_stream_all_cores(vols, kind: str, reps: int = 3):
+    """The whole mixed-size stream on every host core: one spawned process per
+    core takes volumes largest first (the reference is single-threaded, so
+    this is its upper CPU rate on the stream).  Median wall time of `reps`
+    passes after one untimed pass."""
+    import multiprocessing as mp
+    import tempfile
+    cores = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+    offs = np.cumsum([0] + [v.size for v in vols])
+    tasks = sorted(((int(offs[i]), v.shape, kind) for i, v in enumerate(vols)),
+                   key=lambda t: -int(np.prod(t[1])))
+    shm = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    with tempfile.TemporaryDirectory(dir=shm) as tmp:
+        path = os.path.join(tmp, "stream.npy")
+        np.save(path, np.concatenate([v.reshape(-1) for v in vols]))
+        with mp.get_context("spawn").Pool(cores, initializer=_stream_worker_init, initargs=(path,)) as pool:
+            pool.map(_stream_worker_label, tasks, chunksize=1)
+            times = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                done = sum(pool.map(_stream_worker_label, tasks, chunksize=1))
+                times.append(time.perf_counter() - t0)
+    t = pystats.median(times)
+    return {"value": done / t / 1e9, "unit": "GVoxels/s", "cores": cores, "kind": kind,
+            "sample": f"all {len(vols)} volumes of the stream ({done} voxels) spread over {cores} spawned "
+                      f"processes, largest first; median of {reps} passes ({t:.3f} s per pass)"}
+
+
 def run_batch(args):
     """The mixed-size stream: N uint16 Voronoi+membrane volumes, every edge
     log-uniform in [16, 256], one seed per 4096 voxels, labels in [1, 65535],
     26-connectivity.  One JSON line: the batched path (one launch per stage,
     replayed CUDA graph, tile pass from the batch autotuner) against one
-    connected_components call per volume, and the oracle's CPU loop on a
-    bounded sample.  Every batched volume is checked against its
-    single-volume result."""
+    connected_components call per volume, the reference's CPU path on one
+    core (a bounded sample) and on every host core (the whole stream).  Every
+    batched volume is checked against its single-volume result."""
     import torch
     import cc3d_gb300 as cc3d
     from cc3d_gb300 import synth
@@ -605,7 +709,7 @@ def run_batch(args):
     for d, (lab, n) in zip(dev, got):
         ref, rn = cc3d.connected_components(d, connectivity=26, return_N=True)
         mismatches += int(rn != n or ref.dtype != lab.dtype or not torch.equal(ref.to(torch.int64), lab.to(torch.int64)))
-    cpu = None
+    cpu = cpu_all = None
     if not args.skip_cpu:
         import oracle
         oracle.build()
@@ -620,12 +724,14 @@ def run_batch(args):
             k += 1
         cpu = {"value": done / t_cpu / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": kind,
                "sample": f"the first {k} volumes of the stream ({done} voxels), one after another"}
+        cpu_all = cpu_stream_all_cores(vols, kind)
     print(json.dumps({
         "metric": "GVoxels/s mixed-size stream, batched vs per-volume (bit-exact)",
         "value": voxels / ms_batch / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_batch,
         "per_volume_loop": {"value": voxels / ms_loop / 1e6, "ms_per_step": ms_loop},
         "speedup_vs_per_volume": ms_loop / ms_batch,
         "tuned": tuned, "mismatched_volumes": mismatches, "cpu_baseline": cpu,
+        "cpu_all_cores": cpu_all,
         "config": {"workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], "
                                "one seed per 4096 voxels, connectivity 26",
                    "voxels": voxels, "generation_s": t_gen},
@@ -684,6 +790,8 @@ def main():
                     help="the mixed-size stream of this many volumes instead of the headline")
     ap.add_argument("--graphs", action="store_true",
                     help="voxel and colour connectivity graphs of the headline volume instead of the headline")
+    ap.add_argument("--statistics", action="store_true",
+                    help="statistics of the headline volume's labels instead of the headline")
     ap.add_argument("--costmodel", type=int, default=0,
                     help="train and evaluate the cost model on this many generated volumes instead of the headline")
     ap.add_argument("--save-params", default="", help="where --costmodel saves the trained parameters")
@@ -705,6 +813,9 @@ def main():
         return
     if args.graphs:
         run_graphs(args)
+        return
+    if args.statistics:
+        run_statistics(args)
         return
     if args.costmodel:
         run_costmodel(args)
