@@ -606,7 +606,7 @@ def run_statistics(args):
     assert exact, "statistics differ from the oracle"
     best = min(times)
     print(json.dumps({
-        "metric": "GVoxels/s statistics of the 512^3 uint32 labels (counts, boxes, centroids; exact)",
+        "metric": f"GVoxels/s statistics of the {SHAPE[0]}^3 uint32 labels (counts, boxes, centroids; exact)",
         "value": voxels / ms / 1e6, "unit": "GVoxels/s", "ms_per_step": ms, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "N": int(N), "exact_vs_oracle": exact,
         "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak, "unit": "GB/s",
@@ -615,8 +615,8 @@ def run_statistics(args):
         "cpu_baseline": {"value": voxels / best / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": "port",
                          "sample": f"the same labels, oracle's numpy restatement, best of {len(times)} "
                                    f"({best:.3f} s)"},
-        "config": {"workload": "labels of the 512^3 uint32 Voronoi volume at connectivity 26 "
-                               "(device tensors in and out)", "l2": "labels (512 MiB) larger than L2"},
+        "config": {"workload": f"labels of the {SHAPE[0]}^3 uint32 Voronoi volume at connectivity 26 "
+                               "(device tensors in and out)", "l2": "labels larger than L2"},
     }), flush=True)
 
 
