@@ -143,7 +143,11 @@ static uint64_t epl_##SUF(const T *in, int64_t sx, int64_t voxels,              
    For 26-connectivity a voxel equal to the voxel below it (z-1) takes that  \
    label and needs no other test: every other backward neighbour it relates  \
    to is also a 26-neighbour of the voxel below, and that pair was already   \
-   united earlier in the scan.  Returns the number of provisional labels.   */ \
+   united earlier in the scan.  By the same argument a voxel equal to the    \
+   voxel behind it (y-1) only tests the three neighbours (dx, +1, -1) that   \
+   are not adjacent to that voxel, and one equal to the voxel on its left    \
+   (x-1) only the four with dx = +1.  Returns the number of provisional      \
+   labels.                                                                   */ \
 static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz, \
                                  int conn, int binary, int periodic,            \
                                  uint32_t *lab, Labels *L) {                    \
@@ -160,6 +164,10 @@ static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz
      Together these define the reference's effective neighbour relation.     */ \
   const int row0_eq = binary && conn == 4;                                      \
   const int below_shortcut = (conn == 26);                                      \
+  /* 26: the backward neighbours not adjacent to the voxel behind (y-1),       \
+     and those not adjacent to the voxel on the left (x-1) */                   \
+  const int64_t d26_behind[3] = {-1 + sx - sxy, sx - sxy, 1 + sx - sxy};        \
+  const int64_t d26_left[4] = {1 - sx - sxy, 1 - sxy, 1 + sx - sxy, 1 - sx};    \
   for (int64_t z = 0; z < sz; z++)                                              \
     for (int64_t y = 0; y < sy; y++) {                                          \
       int64_t row = sx * (y + sy * z);                                          \
@@ -174,6 +182,25 @@ static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz
         }                                                                       \
         int interior = yz_in && x >= 1 && x + 1 < sx;                           \
         uint32_t cur = 0;                                                       \
+        if (below_shortcut && interior) {                                       \
+          const int64_t *rest = NULL;                                           \
+          int nrest = 0;                                                        \
+          if (EQV(v, in[i - sx])) {                                             \
+            cur = lab[i - sx]; rest = d26_behind; nrest = 3;                    \
+          } else if (EQV(v, in[i - 1])) {                                       \
+            cur = lab[i - 1]; rest = d26_left; nrest = 4;                       \
+          }                                                                     \
+          if (nrest) {                                                          \
+            for (int k = 0; k < nrest; k++) {                                   \
+              const int64_t j = i + rest[k];                                    \
+              if (!EQV(v, in[j])) continue;                                     \
+              const uint32_t l = lab[j];                                        \
+              if (l != cur) cur = lab_unite(L, cur, l);                         \
+            }                                                                   \
+            lab[i] = cur;                                                       \
+            continue;                                                           \
+          }                                                                     \
+        }                                                                       \
         for (int k = 0; k < noff; k++) {                                        \
           if (!interior) {                                                      \
             int64_t nx = x + off[k][0], ny = y + off[k][1], nz = z + off[k][2]; \
@@ -302,6 +329,52 @@ static void store_label(void *out, int out_dtype, int64_t i, uint64_t lab) {
   }
 }
 
+/* Provisional labels live in the output itself when it is uint32 (as the
+   reference's labellers write into out_labels), else in a scratch array. */
+static uint32_t *provisional_buffer(void *out, int out_dtype, int64_t voxels) {
+  if (out_dtype == DT_U32) return (uint32_t *)out;
+  return (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+}
+
+static void release_provisional(uint32_t *lab, void *out) {
+  if ((void *)lab != out) free(lab);
+}
+
+/* Second pass: out[i] = fin[lab[i]] in the output's type, where fin maps a
+   provisional label to its component number and fin[0] = 0.  lab may be the
+   output itself (uint32): each element is read before it is overwritten. */
+static void write_labels(void *out, int out_dtype, const uint32_t *lab, const uint32_t *fin,
+                         int64_t voxels) {
+  switch (out_dtype) {
+    case DT_U16: {
+      uint16_t *o = (uint16_t *)out;
+      for (int64_t i = 0; i < voxels; i++) o[i] = (uint16_t)fin[lab[i]];
+      break;
+    }
+    case DT_U32: {
+      uint32_t *o = (uint32_t *)out;
+      for (int64_t i = 0; i < voxels; i++) o[i] = fin[lab[i]];
+      break;
+    }
+    default: {
+      uint64_t *o = (uint64_t *)out;
+      for (int64_t i = 0; i < voxels; i++) o[i] = fin[lab[i]];
+      break;
+    }
+  }
+}
+
+/* Turns the flattened forest (par[p] = root of p) into fin[p] = component
+   number of p, in place, given ren[root] = number; fin[0] = 0.  Returns the
+   table to index with (a one-entry zero table when there are no labels). */
+static const uint32_t *finish_table(Labels *L, const uint32_t *ren) {
+  static const uint32_t none[1] = {0};
+  if (!L->par) return none;
+  for (uint32_t p = 1; p <= L->n; p++) L->par[p] = ren[L->par[p]];
+  L->par[0] = 0;
+  return L->par;
+}
+
 /* Estimated provisional label count and first/last foreground row
  * (cc3d/cc3d.hpp:287-315).  Returns (uint64_t)-1 on an unknown dtype. */
 uint64_t oracle_epl(const void *in, int dtype, int64_t sx, int64_t voxels,
@@ -361,7 +434,7 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     if (L > outmax) L = outmax;
     if (P >= L) return -5;
   }
-  uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+  uint32_t *lab = provisional_buffer(out, out_dtype, voxels);
   if (!lab) return -4;
   Labels L = {NULL, 0, 0, 0};
   int (*fg)(const void *, int64_t) = NULL;
@@ -379,14 +452,14 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     CASE(DT_F32, f32, float)
     CASE(DT_F64, f64, double)
 #undef CASE
-    default: free(lab); return -1;
+    default: release_provisional(lab, out); return -1;
   }
-  if (L.oom) { free(lab); free(L.par); return -4; }
+  if (L.oom) { release_provisional(lab, out); free(L.par); return -4; }
   /* flatten: parents are smaller than children, so one increasing pass
      leaves every label pointing at its root */
   for (uint32_t p = 1; p <= L.n; p++) L.par[p] = L.par[L.par[p]];
   uint32_t *ren = (uint32_t *)calloc((size_t)L.n + 1, sizeof(uint32_t));
-  if (!ren && L.n) { free(lab); free(L.par); return -4; }
+  if (!ren && L.n) { release_provisional(lab, out); free(L.par); return -4; }
   uint64_t n = 0;
   if (binary && connectivity == 8) {
     /* block-raster numbering: visit 2x2 blocks in raster order; a component
@@ -408,14 +481,11 @@ int oracle_connected_components(const void *in, int dtype, int64_t sx,
     for (uint32_t p = 1; p <= L.n; p++)
       if (L.par[p] == p) ren[p] = (uint32_t)++n;
   }
-  for (int64_t i = 0; i < voxels; i++) {
-    uint32_t l = lab[i];
-    store_label(out, out_dtype, i, l ? ren[L.par[l]] : 0);
-  }
+  write_labels(out, out_dtype, lab, finish_table(&L, ren), voxels);
   (void)fg;
   free(ren);
   free(L.par);
-  free(lab);
+  release_provisional(lab, out);
   *N = n;
   return 0;
 }
@@ -542,7 +612,7 @@ int oracle_connected_components_continuous(const void *in, int dtype, int64_t sx
   *N = 0;
   if (voxels == 0) return 0;
   if (voxels >= (int64_t)0xFFFFFFFFLL) return -3;
-  uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)voxels);
+  uint32_t *lab = provisional_buffer(out, out_dtype, voxels);
   if (!lab) return -4;
   Labels L = {NULL, 0, 0, 0};
   switch (dtype) {
@@ -562,22 +632,19 @@ int oracle_connected_components_continuous(const void *in, int dtype, int64_t sx
     CASE(DT_F32, f32, float)
     CASE(DT_F64, f64, double)
 #undef CASE
-    default: free(lab); return -1;
+    default: release_provisional(lab, out); return -1;
   }
-  if (L.oom) { free(lab); free(L.par); return -4; }
+  if (L.oom) { release_provisional(lab, out); free(L.par); return -4; }
   for (uint32_t p = 1; p <= L.n; p++) L.par[p] = L.par[L.par[p]];
   uint32_t *ren = (uint32_t *)calloc((size_t)L.n + 1, sizeof(uint32_t));
-  if (!ren && L.n) { free(lab); free(L.par); return -4; }
+  if (!ren && L.n) { release_provisional(lab, out); free(L.par); return -4; }
   uint64_t n = 0;
   for (uint32_t p = 1; p <= L.n; p++)
     if (L.par[p] == p) ren[p] = (uint32_t)++n;
-  for (int64_t i = 0; i < voxels; i++) {
-    const uint32_t l = lab[i];
-    store_label(out, out_dtype, i, l ? ren[L.par[l]] : 0);
-  }
+  write_labels(out, out_dtype, lab, finish_table(&L, ren), voxels);
   free(ren);
   free(L.par);
-  free(lab);
+  release_provisional(lab, out);
   *N = n;
   return 0;
 }
