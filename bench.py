@@ -421,8 +421,9 @@ def run_gpu(args, world, rank, local):
         with open(tp) as f:
             traffic = json.load(f).get(dom)
 
+    # the CPU baseline is one process's figure: timed at N = 1 only
     cpu = None
-    if rank == 0 and not args.skip_cpu:
+    if world == 1 and not args.skip_cpu:
         cpu = cpu_reference(vol)
 
     launches_per_step = 8  # tile pass, edge merge, 3 scan kernels + tile reduction, resolve, write
