@@ -61,3 +61,20 @@ def test_port_matches_reference_random(seed):
             assert np.array_equal(o[0][fg], r[0][fg])
         else:
             assert np.array_equal(o[0], r[0])
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not compiled here")
+@pytest.mark.parametrize("conn", [26, 18, 6])
+def test_port_matches_reference_voronoi(conn):
+    """Cell-like volumes (Voronoi with salt), where most voxels repeat the one
+    below, behind or to the left: the 26-connected shortcuts of the port."""
+    from cc3d_gb300 import synth
+    for it, dt in enumerate((np.uint16, np.uint32, np.float32)):
+        vol = synth.voronoi_volume((37, 45, 70), 30 + 40 * it, 60000, seed=conn + it, dtype=dt, salt=0.03)
+        if it == 1:
+            vol = np.asfortranarray(vol)
+        for binary in (False, True):
+            o = oracle.connected_components(vol, connectivity=conn, binary_image=binary, return_N=True)
+            r = oracle.connected_components(vol, connectivity=conn, binary_image=binary, return_N=True,
+                                            backend="reference")
+            assert o[1] == r[1] and o[0].dtype == r[0].dtype and np.array_equal(o[0], r[0]), (dt, binary)
