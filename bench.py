@@ -55,8 +55,6 @@ SHAPE = (512, 512, 512)  # --size changes it for profiling captures only
 N_SEEDS = 4096
 LABEL_MAX = 1 << 20
 CONN = 26
-
-
 HBM_SPEC_GBS = 7900.0  # GB300 HBM3e nominal bandwidth; the roofline's peak is the measured copy rate
 
 
