@@ -69,6 +69,10 @@ def _lib(kind: str):
         lib.oracle_connected_components.restype = ctypes.c_int
         lib.oracle_epl.argtypes = [ctypes.c_void_p, ctypes.c_int, i64, i64, i64p, i64p]
         lib.oracle_epl.restype = ctypes.c_uint64
+        vp = ctypes.c_void_p
+        lib.oracle_statistics.argtypes = [vp, ctypes.c_int, i64, i64, i64, ctypes.c_int, ctypes.c_uint64,
+                                          vp, vp, vp, vp]
+        lib.oracle_statistics.restype = ctypes.c_int
         lib.oracle_connected_components_continuous.argtypes = [
             ctypes.c_void_p, ctypes.c_int, i64, i64, i64, ctypes.c_int, ctypes.c_void_p,
             ctypes.c_void_p, ctypes.c_int, u64p]
@@ -325,7 +329,9 @@ def _delta_bytes(delta, cd: np.dtype):
 
 
 def statistics(out_labels: np.ndarray, no_slice_conversion: bool = False) -> dict:
-    """numpy restatement of cc3d.statistics (fastcc3d.pyx:681-938)."""
+    """Restatement of cc3d.statistics (fastcc3d.pyx:681-938): the argument
+    checks, output dtypes and slices here, the per-voxel pass in C
+    (oracle_statistics, fastcc3d.pyx:767-938)."""
     while out_labels.ndim < 2:
         out_labels = out_labels[..., np.newaxis]
     if out_labels.dtype == bool:
@@ -348,29 +354,29 @@ def statistics(out_labels: np.ndarray, no_slice_conversion: bool = False) -> dic
     ndim = out_labels.ndim
     shape = out_labels.shape
     bdt = np.uint32 if any(s > np.iinfo(np.uint16).max for s in (list(shape) + [1])[:3]) else np.uint16
-    idx = np.indices(shape, dtype=np.int64)
-    # labels and coordinates raveled in the same (C) order; integer sums are
-    # exact, so the accumulation order of the reference does not matter.
-    lab = out_labels.astype(np.int64).reshape(-1)
-    coords = [c.reshape(-1) for c in idx]
-    counts64 = np.bincount(lab, minlength=N + 1)
-    counts = counts64.astype(np.uint32)
+    # one pass of the C restatement over the buffer in its memory order
+    if out_labels.flags.c_contiguous:
+        buf, c_order = out_labels, 1
+    elif out_labels.flags.f_contiguous:
+        buf, c_order = out_labels, 0
+    else:
+        buf, c_order = np.ascontiguousarray(out_labels), 1
+    d0, d1 = int(shape[0]), int(shape[1])
+    d2 = int(shape[2]) if ndim > 2 else 1
+    counts = np.empty(N + 1, dtype=np.uint32)
+    bmin = np.empty((N + 1, 3), dtype=np.uint32)
+    bmax_ = np.empty((N + 1, 3), dtype=np.uint32)
+    cent3 = np.empty((N + 1, 3), dtype=np.float64)
+    rc = _lib("port").oracle_statistics(
+        buf.ctypes.data, buf.dtype.itemsize, d0, d1, d2, c_order, N, counts.ctypes.data,
+        bmin.ctypes.data, bmax_.ctypes.data, cent3.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle statistics failed with code {rc}")
     bmax = np.iinfo(bdt).max
     bb = np.zeros((N + 1, 2 * ndim), dtype=bdt)
-    cent = np.zeros((N + 1, ndim), dtype=np.float64)
-    for a in range(ndim):
-        mins = np.full(N + 1, bmax, dtype=np.int64)
-        maxs = np.zeros(N + 1, dtype=np.int64)
-        np.minimum.at(mins, lab, coords[a])
-        np.maximum.at(maxs, lab, coords[a])
-        bb[:, 2 * a] = mins.astype(bdt)
-        bb[:, 2 * a + 1] = maxs.astype(bdt)
-        s = np.zeros(N + 1, dtype=np.int64)
-        np.add.at(s, lab, coords[a])
-        cent[:, a] = s.astype(np.float64)
-    cnt_d = counts.astype(np.float64)
-    with np.errstate(invalid="ignore", divide="ignore"):
-        cent = np.where(cnt_d[:, None] == 0, np.nan, cent / np.where(cnt_d == 0, 1, cnt_d)[:, None])
+    bb[:, 0::2] = np.minimum(bmin[:, :ndim], bmax).astype(bdt)  # absent labels keep the dtype max
+    bb[:, 1::2] = bmax_[:, :ndim].astype(bdt)
+    cent = np.ascontiguousarray(cent3[:, :ndim])
     output = {"voxel_counts": counts, "bounding_boxes": bb, "centroids": cent}
     if no_slice_conversion:
         return output

@@ -375,6 +375,71 @@ static const uint32_t *finish_table(Labels *L, const uint32_t *ren) {
   return L->par;
 }
 
+/* Per-label voxel counts, bounding boxes and coordinate sums of a label
+ * array: a restatement of _statistics_helper2d/3d (cc3d/fastcc3d.pyx:767-938).
+ * Axes are the array's own (x = axis 0, y = axis 1, z = axis 2, extents d0, d1,
+ * d2; a 2D array has d2 = 1); c_order says whether the buffer is C or Fortran
+ * ordered.  One pass in memory order: counts[l] (uint32, wrapping like the
+ * reference's), bmin/bmax[3 l + a] (bmin starts at 0xFFFFFFFF, bmax at 0), and
+ * centroids[3 l + a] = sum of coordinates / count, NaN for a count of 0.  The
+ * reference adds coordinates into a double one by one; every partial sum is an
+ * integer below 2^53, so the exact 64-bit sums divided once are the same
+ * doubles.  Returns 0, -1 for a label above N or a bad width, -4 when out of
+ * memory. */
+#define STATS_PASS(T)                                                            \
+  do {                                                                           \
+    const T *lab = (const T *)labels;                                            \
+    int64_t i = 0;                                                               \
+    if (c_order) {                                                               \
+      for (int64_t x = 0; x < d0; x++)                                           \
+        for (int64_t y = 0; y < d1; y++)                                         \
+          for (int64_t z = 0; z < d2; z++, i++) STATS_VOXEL((uint64_t)lab[i]);   \
+    } else {                                                                     \
+      for (int64_t z = 0; z < d2; z++)                                           \
+        for (int64_t y = 0; y < d1; y++)                                         \
+          for (int64_t x = 0; x < d0; x++, i++) STATS_VOXEL((uint64_t)lab[i]);   \
+    }                                                                            \
+  } while (0)
+#define STATS_VOXEL(L)                                                           \
+  do {                                                                           \
+    const uint64_t l = (L);                                                      \
+    if (l > N) { bad = 1; break; }                                               \
+    const uint32_t c[3] = {(uint32_t)x, (uint32_t)y, (uint32_t)z};               \
+    counts[l]++;                                                                 \
+    for (int a = 0; a < 3; a++) {                                                \
+      if (c[a] < bmin[3 * l + a]) bmin[3 * l + a] = c[a];                        \
+      if (c[a] > bmax[3 * l + a]) bmax[3 * l + a] = c[a];                        \
+      sums[3 * l + a] += c[a];                                                   \
+    }                                                                            \
+  } while (0)
+int oracle_statistics(const void *labels, int label_bytes, int64_t d0, int64_t d1, int64_t d2,
+                      int c_order, uint64_t N, uint32_t *counts, uint32_t *bmin, uint32_t *bmax,
+                      double *centroids) {
+  const uint64_t n1 = N + 1;
+  uint64_t *sums = (uint64_t *)calloc((size_t)(3 * n1), sizeof(uint64_t));
+  if (!sums) return -4;
+  for (uint64_t l = 0; l < n1; l++) {
+    counts[l] = 0;
+    for (int a = 0; a < 3; a++) { bmin[3 * l + a] = 0xFFFFFFFFu; bmax[3 * l + a] = 0; }
+  }
+  int bad = 0;
+  switch (label_bytes) {
+    case 1: STATS_PASS(uint8_t); break;
+    case 2: STATS_PASS(uint16_t); break;
+    case 4: STATS_PASS(uint32_t); break;
+    case 8: STATS_PASS(uint64_t); break;
+    default: bad = 1;
+  }
+  if (!bad)
+    for (uint64_t l = 0; l < n1; l++)
+      for (int a = 0; a < 3; a++)
+        centroids[3 * l + a] = counts[l] ? (double)sums[3 * l + a] / (double)counts[l] : NAN;
+  free(sums);
+  return bad ? -1 : 0;
+}
+#undef STATS_VOXEL
+#undef STATS_PASS
+
 /* Estimated provisional label count and first/last foreground row
  * (cc3d/cc3d.hpp:287-315).  Returns (uint64_t)-1 on an unknown dtype. */
 uint64_t oracle_epl(const void *in, int dtype, int64_t sx, int64_t voxels,

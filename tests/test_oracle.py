@@ -78,3 +78,49 @@ def test_port_matches_reference_voronoi(conn):
             r = oracle.connected_components(vol, connectivity=conn, binary_image=binary, return_N=True,
                                             backend="reference")
             assert o[1] == r[1] and o[0].dtype == r[0].dtype and np.array_equal(o[0], r[0]), (dt, binary)
+
+
+def _numpy_statistics(labels):
+    """Independent numpy tables for statistics: exact integer reductions."""
+    a = labels if labels.ndim >= 2 else labels[:, None]
+    N = int(a.max())
+    lab = a.astype(np.int64).reshape(-1)
+    coords = [c.reshape(-1) for c in np.indices(a.shape, dtype=np.int64)]
+    counts = np.bincount(lab, minlength=N + 1)
+    bdt = np.uint32 if any(s > 65535 for s in a.shape) else np.uint16
+    bb = np.zeros((N + 1, 2 * a.ndim), dtype=bdt)
+    cent = np.full((N + 1, a.ndim), np.nan)
+    for ax in range(a.ndim):
+        mins = np.full(N + 1, np.iinfo(bdt).max, np.int64)
+        maxs = np.zeros(N + 1, np.int64)
+        np.minimum.at(mins, lab, coords[ax])
+        np.maximum.at(maxs, lab, coords[ax])
+        bb[:, 2 * ax], bb[:, 2 * ax + 1] = mins, maxs
+        sums = np.zeros(N + 1, np.int64)
+        np.add.at(sums, lab, coords[ax])
+        present = counts > 0
+        cent[present, ax] = sums[present].astype(np.float64) / counts[present]
+    return counts.astype(np.uint32), bb, cent
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_statistics_pass_matches_numpy(seed):
+    rng = np.random.default_rng(50 + seed)
+    for it in range(40):
+        dims = int(rng.integers(1, 4))
+        shape = tuple(int(s) for s in rng.integers(1, 20 if dims == 3 else 60, dims))
+        if it == 0:
+            shape = (70000,)  # an axis longer than 65535: uint32 boxes
+        dt = (np.uint8, np.uint16, np.uint32, np.uint64, np.int32)[it % 5]
+        strided = dims == 3 and rng.random() < 0.3
+        final = int(np.prod(shape)) if not strided else shape[0] * ((shape[1] + 1) // 2) * shape[2]
+        a = rng.integers(0, max(1, min(final, 40)), shape).astype(dt)
+        if dims > 1 and rng.random() < 0.5:
+            a = np.asfortranarray(a)
+        if strided:
+            a = a[:, ::2, :]  # neither C nor Fortran contiguous
+        got = oracle.statistics(a, no_slice_conversion=True)
+        counts, bb, cent = _numpy_statistics(np.asarray(a))
+        assert np.array_equal(got["voxel_counts"], counts), (shape, dt)
+        assert got["bounding_boxes"].dtype == bb.dtype and np.array_equal(got["bounding_boxes"], bb), (shape, dt)
+        assert np.array_equal(got["centroids"], cent, equal_nan=True), (shape, dt)
