@@ -166,6 +166,19 @@ def make_volume(rank: int) -> np.ndarray:
     return synth.voronoi_volume(SHAPE, N_SEEDS, LABEL_MAX, seed=1 + rank, dtype=np.uint32)
 
 
+def host_cpu_model() -> str:
+    """The host CPU's model name (lscpu), else the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_reference(vol: np.ndarray, budget_s: float = 20.0):
     """Time the reference's CPU path (compiled reference if present, else the
     oracle's C port) on the full workload volume, best of up to 3 runs."""
@@ -180,7 +193,8 @@ def cpu_reference(vol: np.ndarray, budget_s: float = 20.0):
         _, N = oracle.connected_components(vol, connectivity=CONN, return_N=True, backend=kind)
         times.append(time.perf_counter() - t0)
     best = min(times)
-    return {"value": vol.size / best / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": kind,
+    return {"value": vol.size / best / 1e9, "unit": "GVoxels/s", "cores": 1, "cpu_model": host_cpu_model(),
+            "kind": kind,
             "sample": f"full 512^3 uint32 volume, 26-conn, best of {len(times)} runs "
                       f"({best:.3f} s per volume, N={N})"}
 
@@ -250,7 +264,8 @@ def run_reference(args, world, rank):
                                "connectivity 26, output uint32",
                    "volumes_per_step": cores, "l2": "input larger than L2"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "GVoxels/s", "cores": cores, "kind": kind,
+        "cpu_baseline": {"value": value, "unit": "GVoxels/s", "cores": cores, "cpu_model": host_cpu_model(),
+                         "kind": kind,
                          "sample": f"{cores} copies of the full 512^3 volume per step, one per core in "
                                    f"parallel processes ({per_volume_s:.3f} s per volume, N={res[0][1]})"},
         "e2e": {"value": value, "unit": "GVoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -615,7 +630,8 @@ def run_statistics(args):
         "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak, "unit": "GB/s",
                      "frac": nbytes / ms / 1e6 / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_step": nbytes},
-        "cpu_baseline": {"value": voxels / best / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": "port",
+        "cpu_baseline": {"value": voxels / best / 1e9, "unit": "GVoxels/s", "cores": 1,
+                         "cpu_model": host_cpu_model(), "kind": "port",
                          "sample": f"the same labels, oracle's numpy restatement, best of {len(times)} "
                                    f"({best:.3f} s)"},
         "config": {"workload": f"labels of the {SHAPE[0]}^3 uint32 Voronoi volume at connectivity 26 "
@@ -666,7 +682,8 @@ def cpu_stream_all_cores(vols, kind: str, reps: int = 3):
                 done = sum(pool.map(_stream_worker_label, tasks, chunksize=1))
                 times.append(time.perf_counter() - t0)
     t = pystats.median(times)
-    return {"value": done / t / 1e9, "unit": "GVoxels/s", "cores": cores, "kind": kind,
+    return {"value": done / t / 1e9, "unit": "GVoxels/s", "cores": cores, "cpu_model": host_cpu_model(),
+            "kind": kind,
             "sample": f"all {len(vols)} volumes of the stream ({done} voxels) spread over {cores} spawned "
                       f"processes, largest first; median of {reps} passes ({t:.3f} s per pass)"}
 
@@ -725,7 +742,8 @@ def run_batch(args):
             t_cpu += time.perf_counter() - t1
             done += vols[k].size
             k += 1
-        cpu = {"value": done / t_cpu / 1e9, "unit": "GVoxels/s", "cores": 1, "kind": kind,
+        cpu = {"value": done / t_cpu / 1e9, "unit": "GVoxels/s", "cores": 1, "cpu_model": host_cpu_model(),
+               "kind": kind,
                "sample": f"the first {k} volumes of the stream ({done} voxels), one after another"}
         cpu_all = cpu_stream_all_cores(vols, kind)
     print(json.dumps({

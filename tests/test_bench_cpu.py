@@ -1,6 +1,7 @@
-"""CPU legs of bench.py that need no GPU: the mixed-size stream labelled by
-the reference's CPU path on every host core (spawned processes reading the
-volumes from one memory-mapped file), which must label every volume."""
+"""CPU legs of bench.py that need no GPU: the single-core baseline of the
+headline line, and the mixed-size stream labelled by the reference's CPU path
+on every host core (spawned processes reading the volumes from one
+memory-mapped file), which must label every volume."""
 import os
 import sys
 
@@ -23,3 +24,15 @@ def test_stream_on_all_cores():
     res = bench.cpu_stream_all_cores(vols, "port", reps=1)
     assert res["cores"] >= 1 and res["kind"] == "port" and res["value"] > 0
     assert f"({sum(v.size for v in vols)} voxels)" in res["sample"]
+
+
+def test_single_core_baseline():
+    """The GPU arm's CPU baseline: the reference's CPU path on one core, best of
+    up to three runs, with the host's CPU model."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from cc3d_gb300 import synth
+    vol = synth.voronoi_volume((40, 48, 56), 24, 1 << 20, seed=3)
+    res = bench.cpu_reference(vol, budget_s=5.0)
+    assert res["cores"] == 1 and res["value"] > 0 and res["cpu_model"]
+    assert res["kind"] in ("reference", "port")

@@ -55,3 +55,4 @@ def test_reference_arm_under_torchrun_two_ranks():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["cpu_model"]
