@@ -143,11 +143,12 @@ static uint64_t epl_##SUF(const T *in, int64_t sx, int64_t voxels,              
    For 26-connectivity a voxel equal to the voxel below it (z-1) takes that  \
    label and needs no other test: every other backward neighbour it relates  \
    to is also a 26-neighbour of the voxel below, and that pair was already   \
-   united earlier in the scan.  By the same argument a voxel equal to the    \
-   voxel behind it (y-1) only tests the three neighbours (dx, +1, -1) that   \
-   are not adjacent to that voxel, and one equal to the voxel on its left    \
-   (x-1) only the four with dx = +1.  Returns the number of provisional      \
-   labels.                                                                   */ \
+   united earlier in the scan.  By the same argument an interior voxel that  \
+   relates to the voxel behind it (y-1) or on its left (x-1) takes that      \
+   label and only tests the backward neighbours not adjacent to it (26: 3    \
+   and 4 of them; 18: 3 and 4, and 2 for the voxel below).  The relation     \
+   is an equivalence (equal values, or both foreground), which the argument  \
+   needs.  Returns the number of provisional labels.                         */ \
 static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz, \
                                  int conn, int binary, int periodic,            \
                                  uint32_t *lab, Labels *L) {                    \
@@ -164,10 +165,27 @@ static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz
      Together these define the reference's effective neighbour relation.     */ \
   const int row0_eq = binary && conn == 4;                                      \
   const int below_shortcut = (conn == 26);                                      \
-  /* 26: the backward neighbours not adjacent to the voxel behind (y-1),       \
-     and those not adjacent to the voxel on the left (x-1) */                   \
-  const int64_t d26_behind[3] = {-1 + sx - sxy, sx - sxy, 1 + sx - sxy};        \
-  const int64_t d26_left[4] = {1 - sx - sxy, 1 - sxy, 1 + sx - sxy, 1 - sx};    \
+  /* shortcuts of interior voxels: a related neighbour (below z-1, behind     \
+     y-1, left x-1) and the backward neighbours not adjacent to it */          \
+  int nsc = 0;                                                                  \
+  int64_t sc_prim[3], sc_rest[3][4];                                            \
+  int sc_n[3];                                                                  \
+  if (conn == 26) {                                                             \
+    /* below: handled before, for every voxel with z > 0 */                     \
+    const int64_t behind[3] = {-1 + sx - sxy, sx - sxy, 1 + sx - sxy};          \
+    const int64_t left[4] = {1 - sx - sxy, 1 - sxy, 1 + sx - sxy, 1 - sx};      \
+    sc_prim[0] = -sx; sc_n[0] = 3; memcpy(sc_rest[0], behind, sizeof(behind));  \
+    sc_prim[1] = -1; sc_n[1] = 4; memcpy(sc_rest[1], left, sizeof(left));       \
+    nsc = 2;                                                                    \
+  } else if (conn == 18 && !row0_eq) {                                          \
+    const int64_t below[2] = {-1 - sx, 1 - sx};                                 \
+    const int64_t behind[3] = {-1 - sxy, 1 - sxy, sx - sxy};                    \
+    const int64_t left[4] = {-sx - sxy, 1 - sxy, sx - sxy, 1 - sx};             \
+    sc_prim[0] = -sxy; sc_n[0] = 2; memcpy(sc_rest[0], below, sizeof(below));   \
+    sc_prim[1] = -sx; sc_n[1] = 3; memcpy(sc_rest[1], behind, sizeof(behind));  \
+    sc_prim[2] = -1; sc_n[2] = 4; memcpy(sc_rest[2], left, sizeof(left));       \
+    nsc = 3;                                                                    \
+  }                                                                             \
   for (int64_t z = 0; z < sz; z++)                                              \
     for (int64_t y = 0; y < sy; y++) {                                          \
       int64_t row = sx * (y + sy * z);                                          \
@@ -182,17 +200,14 @@ static uint32_t first_pass_##SUF(const T *in, int64_t sx, int64_t sy, int64_t sz
         }                                                                       \
         int interior = yz_in && x >= 1 && x + 1 < sx;                           \
         uint32_t cur = 0;                                                       \
-        if (below_shortcut && interior) {                                       \
-          const int64_t *rest = NULL;                                           \
-          int nrest = 0;                                                        \
-          if (EQV(v, in[i - sx])) {                                             \
-            cur = lab[i - sx]; rest = d26_behind; nrest = 3;                    \
-          } else if (EQV(v, in[i - 1])) {                                       \
-            cur = lab[i - 1]; rest = d26_left; nrest = 4;                       \
-          }                                                                     \
-          if (nrest) {                                                          \
-            for (int k = 0; k < nrest; k++) {                                   \
-              const int64_t j = i + rest[k];                                    \
+        if (nsc && interior) {                                                  \
+          int hit = -1;                                                         \
+          for (int q = 0; q < nsc; q++)                                         \
+            if (EQV(v, in[i + sc_prim[q]])) { hit = q; break; }                 \
+          if (hit >= 0) {                                                       \
+            cur = lab[i + sc_prim[hit]];                                        \
+            for (int k = 0; k < sc_n[hit]; k++) {                               \
+              const int64_t j = i + sc_rest[hit][k];                            \
               if (!EQV(v, in[j])) continue;                                     \
               const uint32_t l = lab[j];                                        \
               if (l != cur) cur = lab_unite(L, cur, l);                         \
