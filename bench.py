@@ -817,7 +817,7 @@ def main():
                     help="train and evaluate the cost model on this many generated volumes instead of the headline")
     ap.add_argument("--save-params", default="", help="where --costmodel saves the trained parameters")
     ap.add_argument("--tile-pass", default="auto",
-                    help="tile-pass configuration of the headline run: auto, runs, scan or "
+                    help="tile-pass configuration of the headline run: auto, list, runs or "
                          "<variant>/<shape> (profiling captures)")
     args = ap.parse_args()
     global SHAPE, N_SEEDS

@@ -17,7 +17,8 @@ import numpy as np
 from . import _native as nat
 from .api import _CODE, _is_torch
 
-VARIANTS = ("runs", "scan")
+VARIANTS = ("list", "runs")
+_VARIANT_BITS = {"runs": 1, "list": 2}
 SHAPES = ("8x8", "4x16", "16x4")   # 3D tiles 32 x TY x TZ; 2D images always use 32 x 64
 _SHAPE_BITS = {"8x8": 0x00, "4x16": 0x10, "16x4": 0x20}
 # configuration index -> name, in the order of cc3d_gpu_tile_config
@@ -25,13 +26,13 @@ CONFIGS = tuple(f"{v}/{s}" for s in SHAPES for v in VARIANTS)
 
 
 def config_code(name: str) -> int:
-    """CC3D_TILE_* code of "auto", "model", "runs", "scan" or "<variant>/<shape>"."""
+    """CC3D_TILE_* code of "auto", "model", "list", "runs" or "<variant>/<shape>"."""
     if name == "auto":
         return 0
     if name == "model":
         return 3
     variant, _, shape = name.partition("/")
-    return {"runs": 1, "scan": 2}[variant] | _SHAPE_BITS[shape or "8x8"]
+    return _VARIANT_BITS[variant] | _SHAPE_BITS[shape or "8x8"]
 
 
 def config_name(code: int) -> str:
@@ -39,12 +40,13 @@ def config_name(code: int) -> str:
         return "auto"
     if code == 3:
         return "model"
-    return f"{VARIANTS[(code & 15) - 1]}/{SHAPES[(code >> 4) & 15]}"
+    variant = {b: v for v, b in _VARIANT_BITS.items()}[code & 15]
+    return f"{variant}/{SHAPES[(code >> 4) & 15]}"
 
 
 def set_tile_pass(name: str) -> str:
-    """Select the calling thread's tile-pass configuration: "auto", "runs",
-    "scan" (32x8x8 tiles) or "<variant>/<shape>" such as "scan/4x16".
+    """Select the calling thread's tile-pass configuration: "auto", "list",
+    "runs" (32x8x8 tiles) or "<variant>/<shape>" such as "runs/4x16".
     "model" lets the learned cost model choose per volume (the parameters
     shipped with the package are loaded if no model was trained or loaded).
     Returns the previous setting."""

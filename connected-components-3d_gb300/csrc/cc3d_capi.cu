@@ -262,12 +262,11 @@ int resolve_tile_pass(int dtype, int eff, int mode, int64_t voxels) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(dtype, eff, mode, size_bucket(voxels)));
   if (it != g_tuned.end()) return it->second;
-  // without tuning data: block-parallel pass; 32 x 16 x 4 tiles for large
-  // volumes at 18/26-connectivity (fewer halo planes per voxel: 3-5 % on
-  // 512^3), 32 x 8 x 8 otherwise (small volumes waste less of a 16-row tile;
-  // on a stream of 16-256 edged volumes 8 x 8 is 1.3x faster)
-  return ((eff == 26 || eff == 18) && voxels >= (int64_t(1) << 24)) ? (CC3D_TILE_RUNS | CC3D_TILE_16x4)
-                                                                    : CC3D_TILE_RUNS;
+  // without tuning data: the list pass; 32 x 16 x 4 tiles for large
+  // volumes at 18/26-connectivity (fewer halo planes per voxel), 32 x 8 x 8
+  // otherwise (small volumes waste less of a 16-row tile)
+  return ((eff == 26 || eff == 18) && voxels >= (int64_t(1) << 24)) ? (CC3D_TILE_LIST | CC3D_TILE_16x4)
+                                                                    : CC3D_TILE_LIST;
 }
 }  // namespace
 
@@ -840,6 +839,7 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   const size_t o_min = cv.take(n1 * 3 * 4);
   const size_t o_max = cv.take(n1 * 3 * 4);
   const size_t o_sum = cv.take(n1 * 3 * 8);
+  const size_t o_err = cv.take(sizeof(unsigned int));
   const size_t o_bb = stage_out ? cv.take(n1 * 2 * ndim * bsz) : 0;
   const size_t o_ce = stage_out ? cv.take(n1 * ndim * 8) : 0;
   if (int rc = reserve(*w, cv.off)) return rc;
@@ -859,6 +859,8 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
   a.bmin = (uint32_t*)(base + o_min);
   a.bmax = (uint32_t*)(base + o_max);
   a.sums = (unsigned long long*)(base + o_sum);
+  a.err = (unsigned int*)(base + o_err);
+  CK(cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s));
   void* dbb = stage_out ? (void*)(base + o_bb) : bboxes;
   double* dce = stage_out ? (double*)(base + o_ce) : centroids;
   CK(launch_stats(a, s));
@@ -868,7 +870,10 @@ int cc3d_gpu_statistics(const void* labels, int dtype, int64_t d0, int64_t d1, i
     CK(cudaMemcpyAsync(bboxes, dbb, n1 * 2 * ndim * bsz, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(centroids, dce, n1 * ndim * 8, cudaMemcpyDeviceToHost, s));
   }
+  CK(cudaMemcpyAsync(w->host_small, a.err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (*(const unsigned int*)w->host_small)
+    return fail(CC3D_ERR_DEVICE, "a label exceeds N = %llu (its voxels were skipped)", (unsigned long long)N);
   return CC3D_OK;
 }
 
@@ -936,9 +941,9 @@ int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t
 
 int cc3d_gpu_tile_config(int index) {
   static const int codes[CC3D_TILE_CONFIGS] = {
-      CC3D_TILE_RUNS | CC3D_TILE_8x8,  CC3D_TILE_SCAN | CC3D_TILE_8x8,
-      CC3D_TILE_RUNS | CC3D_TILE_4x16, CC3D_TILE_SCAN | CC3D_TILE_4x16,
-      CC3D_TILE_RUNS | CC3D_TILE_16x4, CC3D_TILE_SCAN | CC3D_TILE_16x4};
+      CC3D_TILE_LIST | CC3D_TILE_8x8,  CC3D_TILE_RUNS | CC3D_TILE_8x8,
+      CC3D_TILE_LIST | CC3D_TILE_4x16, CC3D_TILE_RUNS | CC3D_TILE_4x16,
+      CC3D_TILE_LIST | CC3D_TILE_16x4, CC3D_TILE_RUNS | CC3D_TILE_16x4};
   if (index < 0 || index >= CC3D_TILE_CONFIGS) return -1;
   return codes[index];
 }

@@ -195,21 +195,6 @@ int encode_input_map(const LabelArgs& a, uint32_t bw, uint32_t bh, uint32_t bd, 
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// the raster scan: one warp per tile, box planes streamed through a TMA ring
-template <typename T, int CONN, int TY, int TZ, int MODE>
-cudaError_t launch_k1_scan(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  using G = ScanGeom<T, CONN, TY, TZ>;
-  CUtensorMap map;
-  const int use_tma = ntiles > 0 ? encode_input_map<T>(a, (uint32_t)G::W, (uint32_t)G::CH, 1u, &map) : 0;
-  const size_t smem = scan_smem_bytes<T, CONN, TY, TZ>();
-  cudaError_t e = cudaFuncSetAttribute(k_tile_scan<T, CONN, TY, TZ, MODE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = (ntiles + kScanWarps - 1) / kScanWarps;
-  k_tile_scan<T, CONN, TY, TZ, MODE><<<(unsigned)blocks, kScanWarps * 32, smem, s>>>(a, map, use_tma);
-  return cudaGetLastError();
-}
-
 // the block-parallel pass: one CTA of 256 threads per tile, its box staged by
 // one TMA copy
 template <typename T, int CONN, int TY, int TZ, int MODE, bool BLOCK8>
@@ -222,11 +207,25 @@ cudaError_t launch_k1_runs(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// the list pass (multilabel and binary relations): one CTA of 256 threads per
+// tile, its box staged by one TMA copy
+template <typename T, int CONN, int TY, int TZ, int MODE>
+cudaError_t launch_k1_list(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  using B = TileBox<CONN, TY, TZ>;
+  CUtensorMap map;
+  const int use_tma =
+      ntiles > 0 ? encode_input_map<T>(a, (uint32_t)BoxRow<T>::W, (uint32_t)B::BY, (uint32_t)B::BZ, &map) : 0;
+  k_tile_list<T, CONN, TY, TZ, MODE><<<(unsigned)ntiles, kThreads, 0, s>>>(a, map, use_tma);
+  return cudaGetLastError();
+}
+
+// the list pass serves the multilabel and binary relations; the reference's
+// binary 4-connected relation runs on the run-union pass
 template <typename T, int CONN, int TY, int TZ, int MODE>
 cudaError_t launch_k1(const LabelArgs& a, int64_t ntiles, int variant, cudaStream_t s) {
-  if (variant == TILE_PASS_RUNS) return launch_k1_runs<T, CONN, TY, TZ, MODE, false>(a, ntiles, s);
-  if (variant == TILE_PASS_SCAN) return launch_k1_scan<T, CONN, TY, TZ, MODE>(a, ntiles, s);
-  return cudaErrorInvalidValue;
+  if constexpr (MODE == MODE_MULTI || MODE == MODE_BINARY)
+    if (variant == TILE_PASS_LIST) return launch_k1_list<T, CONN, TY, TZ, MODE>(a, ntiles, s);
+  return launch_k1_runs<T, CONN, TY, TZ, MODE, false>(a, ntiles, s);
 }
 
 // 3D tiles of 2048 voxels: 32 x TY x TZ with TY * TZ = 64

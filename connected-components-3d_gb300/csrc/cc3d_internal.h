@@ -6,28 +6,29 @@
 #include <cuda_runtime.h>
 
 #include "cc3d_label.cuh"
-#include "cc3d_scan.cuh"
 #include "cc3d_tile.cuh"
+#include "cc3d_tile_list.cuh"
 
 namespace cc3dgpu {
 
 // per-dtype launchers of the tile labeller and the periodic wrap unions
 // (one translation unit per element type: label_<type>.cu)
-// tile-pass variants: the block-parallel pass (k_tile_runs) and the
-// warp-per-tile raster scan (k_tile_scan)
+// tile-pass variants: the list pass (k_tile_list: multilabel and binary
+// relations) and the run-union pass (k_tile_runs: every relation mode)
 constexpr int TILE_PASS_RUNS = 1;
-constexpr int TILE_PASS_SCAN = 2;
+constexpr int TILE_PASS_LIST = 2;
 
 // A tile-pass configuration (the CC3D_TILE_* codes of include/cc3d_gpu.h):
 // variant in bits 0-3, 3D tile shape in bits 4-7 (0: 32x8x8, 1: 32x4x16,
 // 2: 32x16x4).  2D images always use 32x64 tiles.
 struct TileCfg {
-  int variant;  // TILE_PASS_RUNS or TILE_PASS_SCAN
+  int variant;  // TILE_PASS_LIST or TILE_PASS_RUNS
   int ty, tz;
 };
 inline TileCfg decode_tile_cfg(int code, bool d3) {
   TileCfg c;
-  c.variant = (code & 15) == TILE_PASS_SCAN ? TILE_PASS_SCAN : TILE_PASS_RUNS;
+  const int v = code & 15;
+  c.variant = v == TILE_PASS_LIST ? TILE_PASS_LIST : TILE_PASS_RUNS;
   const int shape = (code >> 4) & 15;
   if (!d3) { c.ty = 64; c.tz = 1; }
   else if (shape == 1) { c.ty = 4; c.tz = 16; }
@@ -36,7 +37,8 @@ inline TileCfg decode_tile_cfg(int code, bool d3) {
   return c;
 }
 inline bool valid_tile_code(int code) {
-  return code == 0 || (((code & 15) == TILE_PASS_RUNS || (code & 15) == TILE_PASS_SCAN) && (code >> 4) <= 2);
+  const int v = code & 15;
+  return code == 0 || ((v == TILE_PASS_RUNS || v == TILE_PASS_LIST) && (code >> 4) <= 2);
 }
 
 #define CC3D_DECLARE_DTYPE_LAUNCHERS(SUF)                                              \
@@ -127,6 +129,7 @@ struct StatsArgs {
   uint32_t* bmin;                // [(N+1) * 3]
   uint32_t* bmax;                // [(N+1) * 3]
   unsigned long long* sums;      // [(N+1) * 3]
+  unsigned int* err;             // set when a label exceeds N (its voxels are skipped)
 };
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s);
 cudaError_t launch_stats_finalize(const StatsArgs& a, void* bboxes, int bbox_dtype,

@@ -92,7 +92,10 @@ __global__ void __launch_bounds__(256) k_stats(StatsArgs a) {
         if constexpr (WIDE) sm[ax] = warp_sum64(mine ? (unsigned long long)c[ax] : 0ull);
         else sm[ax] = __reduce_add_sync(FULL, mine ? c[ax] : 0u);
       }
-      if (lane == leader) {
+      if (lane == leader && ll > a.N) {
+        // a label above the caller's N has no table row: skip it and report
+        atomicOr(a.err, 1u);
+      } else if (lane == leader) {
         int slot = -1;
         if (ll == 0) {
           slot = 0;

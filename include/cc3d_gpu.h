@@ -200,6 +200,9 @@ int cc3d_gpu_label_minmax(
  *              (min, max) per axis; mins start at the type's maximum.
  *   centroids: float64 [N+1][ndim]; NaN where the count is 0.
  * Output buffers are host or device memory per CC3D_OUT_DEVICE.
+ * N must be at least the largest label (the reference computes it as the
+ * maximum); voxels whose label exceeds N are skipped and the call returns
+ * CC3D_ERR_DEVICE.
  */
 int cc3d_gpu_statistics(
     const void* labels, int dtype, int64_t d0, int64_t d1, int64_t d2,
@@ -277,25 +280,29 @@ int cc3d_gpu_run_starts_copy(uint64_t* positions, uint64_t* labels, uint64_t nst
  * reference, which has a single CPU algorithm per connectivity.  Every
  * configuration gives identical labels; they differ only in speed.
  * A configuration code is a variant ORed with a 3D tile shape:
+ *   CC3D_TILE_LIST  one 256-thread block per tile: each row is related to
+ *                   its primary neighbour row by one ballot; voxels that
+ *                   relation does not decide go to per-warp lists and are
+ *                   handled one per lane (multilabel and binary relations;
+ *                   the reference's binary 4-connected relation falls back
+ *                   to CC3D_TILE_RUNS).
  *   CC3D_TILE_RUNS  one 256-thread block per tile: rows cut into runs by
- *                   ballots, unions of overlapping runs in a shared-memory
- *                   union-find.
- *   CC3D_TILE_SCAN  one warp per tile scanning its rows in raster order, fed
- *                   by TMA: runs copy the root of their backward neighbours;
- *                   unions only where two labels meet.
+ *                   ballots, every neighbour row related by ballots, unions
+ *                   of overlapping runs in a shared-memory union-find (every
+ *                   relation mode).
  *   CC3D_TILE_8x8 / _4x16 / _16x4   3D tiles of 32 x 8 x 8, 32 x 4 x 16 or
  *                   32 x 16 x 4 voxels (x y z).  2D images always use 32 x 64.
  * Binary 8-connected images always use CC3D_TILE_RUNS (2x2-block numbering).
  *
  * cc3d_gpu_set_tile_pass: the calling thread's configuration (CC3D_TILE_AUTO
- *   = the autotuned choice for the volume's class, else RUNS | 16x4 for
- *   volumes of 2^24 voxels or more at 18/26-connectivity and RUNS | 8x8
+ *   = the autotuned choice for the volume's class, else LIST | 16x4 for
+ *   volumes of 2^24 voxels or more at 18/26-connectivity and LIST | 8x8
  *   otherwise); returns
  *   the previous setting, or CC3D_ERR_INVALID for an unknown code.
  * cc3d_gpu_tile_pass_choice: the configuration a labelling of this volume
  *   would use now.
  * cc3d_gpu_tile_config: code of configuration `index` in 0..CC3D_TILE_CONFIGS-1
- *   (RUNS|8x8, SCAN|8x8, RUNS|4x16, SCAN|4x16, RUNS|16x4, SCAN|16x4).
+ *   (LIST|8x8, RUNS|8x8, LIST|4x16, RUNS|4x16, LIST|16x4, RUNS|16x4).
  * cc3d_gpu_autotune: times every configuration on `in` (2D: the first two;
  *   best of `repeats` after one warm-up run each), records the fastest for
  *   the volume's class (dtype, effective connectivity, binary or not, voxel
@@ -306,7 +313,7 @@ int cc3d_gpu_run_starts_copy(uint64_t* positions, uint64_t* labels, uint64_t nst
  */
 #define CC3D_TILE_AUTO 0
 #define CC3D_TILE_RUNS 1
-#define CC3D_TILE_SCAN 2
+#define CC3D_TILE_LIST 2
 #define CC3D_TILE_8x8 0x00
 #define CC3D_TILE_4x16 0x10
 #define CC3D_TILE_16x4 0x20
@@ -433,8 +440,8 @@ int cc3d_gpu_autotune_batch(const cc3d_gpu_volume* volumes, int n, int dtype, in
  *     calls whose GPU work overlaps (other threads, unordered streams) race
  *     and corrupt each other's results.
  *   - Allocates no device or pinned memory; N and the device error word come
- *     back through host stack memory, and the call returns when labels are
- *     written.
+ *     back through host stack memory, and the call synchronizes `stream`
+ *     before it returns, with the labels written.
  */
 #define CC3D_NOALLOC_SCRATCH_BYTES 41943040u /* 40 MiB */
 int cc3d_gpu_connected_components3d_noalloc(

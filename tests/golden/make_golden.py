@@ -2,7 +2,7 @@
 
 Run in a container that has the reference source tree, Cython and g++:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference source tree>   (or set CC3D_REFERENCE)
 
 It compiles the reference's Cython extension out of tree (into a scratch
 directory under /tmp, never into the reference or this repository), imports it,
@@ -297,7 +297,8 @@ def stats_cases(rec: Recorder):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CC3D_REFERENCE"), required="CC3D_REFERENCE" not in os.environ,
+                    help="the reference source tree (default: $CC3D_REFERENCE)")
     ap.add_argument("--random", type=int, default=700)
     args = ap.parse_args()
     sys.path.insert(0, build_reference(args.ref))

@@ -18,7 +18,7 @@ import __graft_entry__ as entry
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ("runs/8x8", "scan/8x8", "runs/4x16", "scan/4x16", "runs/16x4", "scan/16x4")
+VARIANTS = ("list/8x8", "runs/8x8", "list/4x16", "runs/4x16", "list/16x4", "runs/16x4")
 
 
 @pytest.fixture(scope="module")

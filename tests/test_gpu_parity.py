@@ -11,8 +11,8 @@ import __graft_entry__ as entry
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module", params=["runs/8x8", "scan/8x8", "runs/4x16", "scan/4x16", "runs/16x4",
-                                        "scan/16x4"])
+@pytest.fixture(scope="module", params=["list/8x8", "runs/8x8", "list/4x16", "runs/4x16", "list/16x4",
+                                        "runs/16x4"])
 def cc3d(request):
     """The package with one tile-pass configuration selected: every parity
     test runs once per configuration."""

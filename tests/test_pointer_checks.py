@@ -41,3 +41,21 @@ def test_host_addresses_are_refused(env):
     # and the checked Python layer still labels the device volume
     lab, N = cc3d.connected_components(dev.view(16, 16, 16), return_N=True)
     assert N == 1
+
+
+def test_statistics_rejects_labels_above_n(env):
+    """statistics takes N from the caller: a label above it must not index past
+    the tables.  Its voxels are skipped and the call reports a device error;
+    the next call with the right N is exact."""
+    cc3d, nat, lib, torch = env
+    lab = torch.arange(64, dtype=torch.uint32, device="cuda").view(4, 4, 4)
+    N = 10  # the real maximum is 63
+    counts = torch.zeros(N + 1, dtype=torch.uint32, device="cuda")
+    bbox = torch.zeros((N + 1) * 6, dtype=torch.uint16, device="cuda")
+    cent = torch.zeros((N + 1) * 3, dtype=torch.float64, device="cuda")
+    rc = lib.cc3d_gpu_statistics(lab.data_ptr(), nat.U32, 4, 4, 4, 3, 1, N, counts.data_ptr(), bbox.data_ptr(),
+                                 nat.U16, cent.data_ptr(), nat.IN_DEVICE | nat.OUT_DEVICE, None)
+    assert rc == nat.ERR_DEVICE and b"exceeds N" in lib.cc3d_gpu_last_error()
+    assert counts.sum().item() == N + 1  # only labels 0..N were counted
+    s = cc3d.statistics(lab, no_slice_conversion=True)
+    assert s["voxel_counts"].cpu().tolist() == [1] * 64

@@ -18,24 +18,24 @@ def cc3d():
 
 def test_choice_follows_the_thread_setting(cc3d):
     vol = np.zeros((40, 50, 60), np.uint32)
-    assert cc3d.set_tile_pass("scan") == "auto"
-    assert cc3d.tile_pass_choice(vol) == "scan/8x8"
-    assert cc3d.set_tile_pass("runs/4x16") == "scan/8x8"
-    assert cc3d.tile_pass_choice(vol) == "runs/4x16"
-    cc3d.set_tile_pass("scan/16x4")
-    assert cc3d.tile_pass_choice(vol) == "scan/16x4"
+    assert cc3d.set_tile_pass("runs") == "auto"
+    assert cc3d.tile_pass_choice(vol) == "runs/8x8"
+    assert cc3d.set_tile_pass("list/4x16") == "runs/8x8"
+    assert cc3d.tile_pass_choice(vol) == "list/4x16"
+    cc3d.set_tile_pass("runs/16x4")
+    assert cc3d.tile_pass_choice(vol) == "runs/16x4"
     # 2D images have one tile shape
-    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "scan/8x8"
+    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "runs/8x8"
     cc3d.set_tile_pass("auto")
     cc3d.autotune_reset()
     # the defaults without tuning data: 32x16x4 tiles for large 18/26-connected volumes
-    assert cc3d.tile_pass_choice(vol) == "runs/8x8"
+    assert cc3d.tile_pass_choice(vol) == "list/8x8"
     big = np.zeros((256, 256, 256), np.uint8)
-    assert cc3d.tile_pass_choice(big) == "runs/16x4"
-    assert cc3d.tile_pass_choice(big, connectivity=18) == "runs/16x4"
-    assert cc3d.tile_pass_choice(big, connectivity=6) == "runs/8x8"
-    # binary 8-connected images always take the block pass (2x2-block numbering)
-    cc3d.set_tile_pass("scan")
+    assert cc3d.tile_pass_choice(big) == "list/16x4"
+    assert cc3d.tile_pass_choice(big, connectivity=18) == "list/16x4"
+    assert cc3d.tile_pass_choice(big, connectivity=6) == "list/8x8"
+    # binary 8-connected images always take the run-union pass (2x2-block numbering)
+    cc3d.set_tile_pass("list")
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs/8x8"
     cc3d.set_tile_pass("auto")
     from cc3d_gb300.tuning import CONFIGS, config_code
@@ -76,4 +76,4 @@ def test_autotune_records_the_fastest_configuration(cc3d):
         cc3d.set_tile_pass("auto")
     img = synth.bernoulli_volume((300, 400), 0.5, seed=3)
     res = cc3d.autotune(img, connectivity=4)
-    assert set(res["ms"]) == {"runs/8x8", "scan/8x8"}
+    assert set(res["ms"]) == {"list/8x8", "runs/8x8"}

@@ -1,15 +1,17 @@
 """The no-allocation entry point (cc3d_gpu_connected_components3d_noalloc)
 against the workspace entry point (cc3d_gpu_connected_components3d), both
-called through the C ABI on device buffers.  Several calls in a row share the
-fixed scratch array, so a call that read what the previous one left behind
-would show up as a mismatch.  Collected last, and written to pass alone in a
-fresh process too."""
+called through the C ABI on device buffers, and against the oracle.  Several
+calls in a row share the fixed scratch array, so a call that read what the
+previous one left behind would show up as a mismatch.  The calls must also
+leave the device's free memory unchanged: that is what the entry point is
+for.  Collected last, and written to pass alone in a fresh process too."""
 import ctypes
 
 import numpy as np
 import pytest
 
 import __graft_entry__ as entry
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -74,6 +76,43 @@ def test_noalloc_matches_workspace_path_on_calls_in_a_row(lib):
         assert n_got == n_ref, name
         assert got.dtype == ref.dtype and np.array_equal(got, ref), name
         assert n_ref > 0, name
+        exp, n_exp = oracle.connected_components(vol, connectivity=conn, return_N=True, binary_image=binary,
+                                                 periodic_boundary=periodic, out_dtype=OUT[out_code])
+        assert n_got == n_exp, name
+        assert np.array_equal(got, exp), name
+
+
+def test_noalloc_leaves_device_memory_unchanged(lib):
+    """After one warm-up call (the module and its scratch array are resident
+    from then on), labelling allocates nothing: every input and output is made
+    first, and the device's free memory is the same after the calls."""
+    import torch
+
+    cases = _cases()
+    bufs = []
+    for name, vol, conn, binary, out_code, periodic in cases:
+        dev = torch.from_numpy(np.ascontiguousarray(vol)).cuda()
+        out = torch.zeros(vol.shape, dtype=getattr(torch, np.dtype(OUT[out_code]).name), device="cuda")
+        bufs.append((dev, out))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def run_all():
+        for (name, vol, conn, binary, out_code, periodic), (dev, out) in zip(cases, bufs):
+            sz, sy, sx = (1,) * (3 - vol.ndim) + tuple(vol.shape)
+            N = ctypes.c_uint64(0)
+            rc = lib.cc3d_gpu_connected_components3d_noalloc(
+                ctypes.c_void_p(dev.data_ptr()), CODES[vol.dtype], sx, sy, sz, int(vol.size), conn,
+                ctypes.c_void_p(out.data_ptr()), out_code, ctypes.byref(N), int(periodic), int(binary), stream)
+            assert rc == 0, (name, lib.cc3d_gpu_last_error())
+
+    run_all()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    run_all()
+    run_all()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_rejects_volumes_beyond_its_scratch(lib):
