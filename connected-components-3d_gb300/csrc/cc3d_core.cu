@@ -176,7 +176,9 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
 
 // ---------------------------------------------------------------- resolve
 // Final label of every component: 1 + rank of its root's key among the
-// surviving keys.  One warp per tile, one lane per component.
+// surviving keys.  A tile's components are named by their root runs (the
+// runs whose component id is their own index).  One warp per tile, one lane
+// per run.
 __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -188,6 +190,7 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
     // a batch numbers each volume from 1: subtract the keys of the volumes before it
     const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
     for (uint32_t c = lane; c < C; c += 32) {
+      if (p.rcomp[node0 + c] != c) continue;  // not a root run: no entry of its own
       const uint32_t R = gfind(p.E, node0 + c, p.ctr);
       const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
       const uint32_t w = key >> 5;
@@ -209,7 +212,6 @@ cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cu
 
 template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
-  k_resolve<<<152 * 16, 256, 0, s>>>(a);
   return launch_write_tiles_t<OUT>(a, out, ntiles, s);
 }
 
@@ -281,15 +283,15 @@ cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// the writer alone, for the tiles [a.tile_base, a.tile_base + count)
+// labels of the tiles [a.tile_base, a.tile_base + count) of a single volume,
+// resolved and written by one block per tile
 template <typename OUT>
 cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  // one block per tile (a resident grid walking the tiles measured slower)
-  if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  if (a.ty == 8 && a.tz == 8) k_write_fused<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 4 && a.tz == 16) k_write_fused<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 16 && a.tz == 4) k_write_fused<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 64 && a.tz == 1) k_write_fused<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

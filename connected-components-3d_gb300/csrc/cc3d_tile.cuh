@@ -26,8 +26,9 @@
 //            neither the voxel before it nor the dx = 0 relation already
 //            joins.  Unions go through small per-warp queues and are run in
 //            dense rounds (lane i takes entry i), every lane at one call site.
-//   phase 3  roots -> dense component ids in tile raster order, run-length
-//            records, component keys, the numbering bitmap, one edge per
+//   phase 3  roots -> component ids (the index of the root run in the
+//            tile's run order), run-length records, component keys, the
+//            numbering bitmap, one edge per
 //            halo run (or halo-column voxel) joined to a tile component --
 //            except where the same-owner voxel just before it (dx = 0, one row
 //            back in y, else in z) has the same value and joined the same
@@ -128,7 +129,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // component ids (phase 3) share their storage with the phase-2 union queues
   __shared__ __align__(16) unsigned short cid[kTV];
   __shared__ uint32_t rootm[NR];
-  __shared__ unsigned short rbase[NR + 1], cbase[NR + 1];
+  __shared__ unsigned short rbase[NR + 1];
   __shared__ uint32_t minblk[BLOCK8 ? kTV : 1];
   static_assert(NW * QN * sizeof(uint32_t) <= sizeof(unsigned short) * kTV,
                 "queues must fit in the component-id storage");
@@ -461,32 +462,31 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     if (lane == 0) {
       rootm[ri] = rm;
       rbase[ri + 1] = (unsigned short)__popc(Sr);
-      cbase[ri + 1] = (unsigned short)__popc(rm);
     }
   }
   __syncthreads();
   if (warp == 0) {
-    // exclusive prefix over the 64 rows (two per lane)
+    // exclusive prefix of the run counts over the 64 rows (two per lane)
     const uint32_t a0 = rbase[2 * lane + 1], a1 = rbase[2 * lane + 2];
-    const uint32_t c0 = cbase[2 * lane + 1], c1 = cbase[2 * lane + 2];
-    uint32_t sa = a0 + a1, sc = c0 + c1;
+    uint32_t sa = a0 + a1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t ya = __shfl_up_sync(FULL, sa, o), yc = __shfl_up_sync(FULL, sc, o);
-      if (lane >= o) { sa += ya; sc += yc; }
+      const uint32_t ya = __shfl_up_sync(FULL, sa, o);
+      if (lane >= o) sa += ya;
     }
     rbase[2 * lane + 1] = (unsigned short)(sa - a1);
     rbase[2 * lane + 2] = (unsigned short)sa;
-    cbase[2 * lane + 1] = (unsigned short)(sc - c1);
-    cbase[2 * lane + 2] = (unsigned short)sc;
-    if (lane == 0) { rbase[0] = 0; cbase[0] = 0; }
+    if (lane == 0) rbase[0] = 0;
   }
   __syncthreads();
+  // a component is named by the index of its root run in the tile's run
+  // order; ids run up to the tile's run count C
   for (int ri = warp; ri < NR; ri += NW) {
     const uint32_t rm = rootm[ri];
-    if ((rm >> lane) & 1u) cid[ri * 32 + lane] = (unsigned short)(cbase[ri] + __popc(rm & lt));
+    if ((rm >> lane) & 1u)
+      cid[ri * 32 + lane] = (unsigned short)(rbase[ri] + __popc(smask[box_row(ri)] & lt));
   }
-  const uint32_t C = cbase[NR];
+  const uint32_t C = rbase[NR];
   if (BLOCK8)
     for (uint32_t c = tid; c < C; c += kThreads) minblk[c] = 0xFFFFFFFFu;
   __syncthreads();
@@ -522,6 +522,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     __syncthreads();
     for (uint32_t c = tid; c < C; c += kThreads) {
       const uint32_t key = minblk[c];
+      if (key == 0xFFFFFFFFu) continue;  // not a root run
       atomicOr(p.bitmap + (key >> 5), 1u << (key & 31));
       p.E[node0 + c] = ((unsigned long long)key << 32) | (node0 + c);
     }

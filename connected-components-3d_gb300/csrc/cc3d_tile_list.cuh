@@ -14,28 +14,33 @@
 //     neighbours is also a neighbour of the primary one, earlier in raster
 //     order, and related to it when related to the voxel, so that pair is
 //     joined by induction over the raster order.  The voxel's own join with
-//     the primary neighbour is one union per pair of runs (this row's run,
-//     the neighbour row's run) where the pair starts.
+//     its link row (below in 3D, behind in 2D) is one union per pair of runs
+//     (this row's run, the link row's run) where the pair starts; the first
+//     such pair of every run is a direct parent link to the link row's run,
+//     so union-find trees are short chains along z.
 //   * The other ("needy") voxels are few (background faces and isolated
-//     values): their x positions go to a per-warp list and each is then
-//     handled by one lane, which tests its remaining backward neighbours
-//     itself.  A voxel that continues a run (equal to its left neighbour)
-//     skips the neighbours that its left neighbour already sees, and a
-//     diagonal relation is skipped where the same neighbour run is already
-//     joined through the dx = 0 relation.
+//     values): they go to a per-warp list and each is then handled by one
+//     lane, which tests its remaining backward neighbours itself.  A voxel
+//     that continues a run (equal to its left neighbour) skips the neighbours
+//     that its left neighbour already sees, and a diagonal relation is skipped
+//     where the same neighbour run is already joined through the dx = 0
+//     relation.
 //   * 6- and 4-connected labellers have no primary neighbour: every row pair
 //     contributes one union per starting pair of runs, found by ballots.
 //
-// Row-level work is therefore a handful of warp instructions per 32-voxel row
-// (two ballots for the run masks, one for the primary relation, two list
-// appends); unions run from the lists with one lane per entry.
+// Indices are 32-bit (tile and node ids fit 32 bits), and the geometry of
+// every box row (its tile, its row inside that tile, its global row, its
+// same-owner predecessor) comes from tables built once per tile.  A
+// component is named by its root run: the smallest node of its tree, i.e.
+// its first run in tile raster order; the name is that run's index in the
+// tile's run order, so no separate component numbering is needed.
 //
-// Phases: 0 box by TMA (or plain loads), node table; 1 run masks of every box
+// Phases: 0 box by TMA (or plain loads), row tables; 1 run masks of every box
 // row, union-find nodes of the run heads, the provisional-label estimate
-// (cc3d/cc3d.hpp:287-315); 2 primary relations and lists, then the unions of
-// the warp's own lists; 3 roots (path-compressed), per-row counts, prefix;
-// 4 records, keys, bitmap, halo edges, the binary labellers' provisional
-// count, per-tile results.
+// (cc3d/cc3d.hpp:287-315); 2a primary relations, direct links, the warp's
+// union list; 2b its unions; 3 roots, run records, keys, bitmap (halo heads
+// are pointed at their roots); 4 halo edges, the binary labellers'
+// provisional count, per-tile results.
 #pragma once
 
 #include "cc3d_tile.cuh"
@@ -88,7 +93,7 @@ template <> struct NeedRels<4> {
 };
 
 template <typename T, int CONN, int TY, int TZ, int MODE>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, 6)
 k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
   static_assert(MODE == MODE_MULTI || MODE == MODE_BINARY, "multilabel or binary relation");
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
@@ -103,29 +108,39 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int NW = kThreads / 32;
   constexpr int NRN = RowNb<CONN>::n;
   constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
-  // a primary neighbour row decides most voxels (box-row offset of the
-  // row-level pair: below in 3D, behind in 2D)
+  // a primary neighbour row decides most voxels (26, 18: below; 8: behind)
   constexpr bool PRIMARY = (CONN == 26 || CONN == 18 || CONN == 8);
-  constexpr int POFF = (CONN == 8) ? -1 : -BY;
+  // the link row: every run's first pair of runs with it becomes a direct
+  // parent link (below in 3D, behind in 2D)
+  constexpr int LOFF = D3 ? -BY : -1;
+  constexpr int LROW0 = D3 ? TY : 1;     // first tile row whose link row is a tile row
   constexpr int QN = (NR / NW) * 32;     // list capacity: every voxel of the warp's rows
   using NRel = NeedRels<CONN>;
+  constexpr int NB = NRel::n;
   static_assert(kTX * NR == kTV, "tile must hold 2048 voxels");
   static_assert(NR == kRowsPerTile, "64 rows per tile");
   static_assert(NR % NW == 0, "rows per warp");
   static_assert(NODES < 16384, "node ids must fit 14 bits");
   static_assert(W <= 256 && BY <= 256 && BZ <= 256, "TMA box dimensions");
-  static_assert(NRB < 256, "box rows fit a byte");
+  static_assert(NRB < 255, "box rows fit a byte");
 
   __shared__ __align__(128) T box[NRB * W];
   __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t smask[NRB], fmask[NRB];
   __shared__ __align__(16) unsigned short par[NODES];
-  __shared__ unsigned short nbase[NRB];  // node id of a box row's voxel 0
-  __shared__ unsigned short plist[NW][QN], nlist[NW][QN];
-  __shared__ uint32_t rootm[NR];
-  __shared__ unsigned short rbase[NR + 1], cbase[NR + 1];
+  // per box row: node id of its voxel 0; the tile holding its 32 voxels and
+  // the row's index inside that tile; the same-owner box row before it (one
+  // back in y, else in z; 255: none); global row index y + sy * z; flags
+  // (bit 0: tile row, bit 1: inside the volume)
+  __shared__ unsigned short nbase[NRB], rloc[NRB];
+  __shared__ uint32_t rtile[NRB], rgrow[NRB];
+  __shared__ unsigned char rprev[NRB], rflag[NRB];
+  // per warp: one entry per voxel of its rows that has unions to run:
+  // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x
+  __shared__ unsigned short ulist[NW][QN];
+  __shared__ unsigned short rbase[NR + 1];  // first run of every tile row
   __shared__ unsigned long long red_epl[NW];
-  __shared__ long long red_first[NW], red_last[NW];
+  __shared__ int red_first[NW], red_last[NW];
   __shared__ unsigned int red_prov[NW];
   __shared__ unsigned int local_err;
   __shared__ unsigned int edge_fill;
@@ -133,27 +148,12 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t tile = p.tile_base + blockIdx.x;
   const TileGeo g = tile_geo(p, tile);
-  const int tx = g.tx;
-  const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
+  const uint32_t utile = (uint32_t)tile;  // tile ids and node ids fit 32 bits
+  const uint32_t node0 = utile * (uint32_t)kTV;
+  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   const uint32_t lt = (1u << lane) - 1u;
 
-  auto is_tile_row = [&](int rb) -> bool {
-    const int by = rb % BY, bz = rb / BY;
-    return by >= 1 && by <= TY && bz >= HZ;
-  };
-  auto tile_row_of = [&](int rb) -> int { return (rb % BY - 1) + TY * (rb / BY - HZ); };
   auto box_row_of = [&](int ri) -> int { return (ri / TY + HZ) * BY + (ri % TY) + 1; };
-  // index of a halo box row among the halo rows (the whole first plane in
-  // 3D, then the two y faces of every tile plane)
-  auto halo_row_of = [&](int rb) -> int {
-    const int by = rb % BY, bz = rb / BY;
-    return bz < HZ ? by : HZ * BY + (bz - HZ) * 2 + (by == 0 ? 0 : 1);
-  };
-  // which neighbouring tile holds a halo row
-  auto row_owner = [&](int rb) -> int {
-    const int by = rb % BY, bz = rb / BY;
-    return (by == 0 ? 0 : (by == BY - 1 ? 2 : 1)) + 3 * (bz < HZ ? 0 : 1);
-  };
   auto at = [&](int rb, int x) -> T { return box[rb * W + PADX + x]; };
   // relation of a foreground voxel with value a and a neighbour b
   auto R = [&](T a, T b) -> bool {
@@ -167,7 +167,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     return dy + BY * dz;
   };
 
-  // ---- phase 0: the box arrives while the node table is set up
+  // ---- phase 0: the box arrives while the row tables are set up
   if (tid == 0) {
     local_err = 0;
     edge_fill = 0;
@@ -201,7 +201,33 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     }
   }
   for (int rb = tid; rb < NRB; rb += kThreads) {
-    nbase[rb] = (unsigned short)(is_tile_row(rb) ? tile_row_of(rb) * 32 : HNODE + halo_row_of(rb) * 32);
+    const int by = rb % BY, bz = rb / BY;
+    const bool trow = by >= 1 && by <= TY && bz >= HZ;
+    const int ty_off = by == 0 ? -1 : (by == BY - 1 ? 1 : 0);
+    const int tz_off = bz < HZ ? -1 : 0;
+    const int ly = by == 0 ? TY - 1 : (by == BY - 1 ? 0 : by - 1);
+    const int lz = bz < HZ ? TZ - 1 : bz - HZ;
+    // which tile holds a box row: its y and z offsets from this tile
+    auto owner = [&](int r) -> int {
+      const int b = r % BY, c = r / BY;
+      return (b == 0 ? 0 : (b == BY - 1 ? 2 : 1)) + 3 * (c < HZ ? 0 : 1);
+    };
+    const int own = (ty_off + 1) + 3 * (tz_off + 1);
+    int prev = 255;
+    if (by > 0 && owner(rb - 1) == own) prev = rb - 1;
+    else if (bz > 0 && owner(rb - BY) == own) prev = rb - BY;
+    const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
+    const bool in_vol = y >= 0 && y < g.sy && z >= 0 && z < g.sz;
+    // halo rows: the whole first plane in 3D, then the two y faces of every
+    // tile plane
+    const int hidx = bz < HZ ? by : HZ * BY + (bz - HZ) * 2 + (by == 0 ? 0 : 1);
+    nbase[rb] = (unsigned short)(trow ? (ly + TY * lz) * 32 : HNODE + hidx * 32);
+    rloc[rb] = (unsigned short)(ly + TY * lz);
+    // (rows outside the volume hold no foreground, so their tile id is unused)
+    rtile[rb] = (uint32_t)(g.tile0 + g.tx + (int64_t)g.ntx * ((g.ty + ty_off) + (int64_t)g.nty * (g.tz + tz_off)));
+    rgrow[rb] = in_vol ? (uint32_t)(y + g.sy * z) : 0u;
+    rprev[rb] = (unsigned char)prev;
+    rflag[rb] = (unsigned char)((trow ? 1 : 0) | (in_vol ? 2 : 0));
     par[CNODE + rb] = (unsigned short)(CNODE + rb);
     par[CNODE + NRB + rb] = (unsigned short)(CNODE + NRB + rb);
   }
@@ -216,7 +242,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
 
   // ---- phase 1: run masks of every box row; the run heads become nodes
   unsigned long long epl_acc = 0;
-  int frb = NRB, lrb = -1;  // first / last box rows with estimate transitions
+  int frb = -1, lrb = -1;  // first / last box rows with estimate transitions
   for (int rb = warp; rb < NRB; rb += NW) {
     const T v = at(rb, lane), vl = at(rb, lane - 1);
     const bool fg = v != T(0);
@@ -234,91 +260,88 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const unsigned short n = (unsigned short)(nbase[rb] + lane);
       par[n] = n;
     }
-    if (MODE == MODE_MULTI && p.want_epl && E && is_tile_row(rb)) {
+    if (MODE == MODE_MULTI && E && (rflag[rb] & 1u)) {
       epl_acc += __popc(E);
-      frb = rb < frb ? rb : frb;
-      lrb = rb > lrb ? rb : lrb;
+      if (frb < 0) frb = rb;
+      lrb = rb;
     }
   }
   __syncthreads();
 
-  // ---- phase 2: row-level relations and the warp's lists, then its unions
-  int pn = 0, nn = 0;  // warp-uniform list fills
-  unsigned short* pl = plist[warp];
-  unsigned short* nl = nlist[warp];
+  // ---- phase 2a: row-level relations.  The first pair of every run with
+  // its link row becomes a direct parent link (to a smaller node, so roots
+  // stay the smallest node of their tree); the other row-level pairs and the
+  // needy voxels go to the warp's list.
+  if (warp == 0) {
+    // exclusive prefix of the run counts over the tile rows (two per lane)
+    const uint32_t a0 = __popc(smask[box_row_of(2 * lane)]), a1 = __popc(smask[box_row_of(2 * lane + 1)]);
+    uint32_t sa = a0 + a1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t ya = __shfl_up_sync(FULL, sa, o);
+      if (lane >= o) sa += ya;
+    }
+    rbase[2 * lane] = (unsigned short)(sa - a0 - a1);
+    rbase[2 * lane + 1] = (unsigned short)(sa - a1);
+    if (lane == 31) rbase[NR] = (unsigned short)sa;
+  }
+  int un = 0;  // warp-uniform list fill
+  unsigned short* ul = ulist[warp];
   for (int ri = warp; ri < NR; ri += NW) {
     const int rb = box_row_of(ri);
+    const int rl = rb + LOFF;
     const T v = at(rb, lane);
-    const uint32_t F = fmask[rb], Sc = smask[rb];
+    const uint32_t F = fmask[rb], Sc = smask[rb], Sl = smask[rl];
     const bool fg = (F >> lane) & 1u;
-    uint32_t P, NEED = 0, km = 1u;
-    if constexpr (PRIMARY) {
-      const uint32_t M = __ballot_sync(FULL, fg && R(v, at(rb + POFF, lane)));
-      P = M & (Sc | smask[rb + POFF] | ~(M << 1));
-      uint32_t cov = M;
-      if constexpr (CONN == 18) cov &= __ballot_sync(FULL, fg && R(v, at(rb - 1, lane)));
-      NEED = F & ~cov;
+    const uint32_t M = __ballot_sync(FULL, fg && R(v, at(rl, lane)));
+    const uint32_t P = M & (Sc | Sl | ~(M << 1));
+    uint32_t NEED = 0, km = 0;
+    if constexpr (CONN == 26 || CONN == 8) {
+      NEED = F & ~M;
+    } else if constexpr (CONN == 18) {
+      NEED = F & ~(M & __ballot_sync(FULL, fg && R(v, at(rb - 1, lane))));
     } else {
-      // behind (and below for 6): one union per starting pair of runs; lane
-      // 0 also relates to the column x0 - 1 of its own row
-      const uint32_t M0 = __ballot_sync(FULL, fg && R(v, at(rb - 1, lane)));
-      const uint32_t P0 = M0 & (Sc | smask[rb - 1] | ~(M0 << 1));
-      uint32_t P1 = 0;
+      // 6: the row behind too; 6 and 4: lane 0 and the column x0 - 1
       if constexpr (CONN == 6) {
-        const uint32_t M1 = __ballot_sync(FULL, fg && R(v, at(rb - BY, lane)));
-        P1 = M1 & (Sc | smask[rb - BY] | ~(M1 << 1));
+        const uint32_t M0 = __ballot_sync(FULL, fg && R(v, at(rb - 1, lane)));
+        km = ((M0 & (Sc | smask[rb - 1] | ~(M0 << 1))) >> lane) & 1u;
       }
-      const bool lc = lane == 0 && fg && R(v, at(rb, -1));
-      km = ((P0 >> lane) & 1u) | (((P1 >> lane) & 1u) << 1) | (lc ? 4u : 0u);
-      P = __ballot_sync(FULL, km != 0u);
+      if (lane == 0 && fg && R(v, at(rb, -1))) km |= 4u;
     }
-    if ((P >> lane) & 1u) pl[pn + __popc(P & lt)] = (unsigned short)((km << 11) | (ri << 5) | lane);
-    pn += __popc(P);
-    if (PRIMARY) {
-      if ((NEED >> lane) & 1u) nl[nn + __popc(NEED & lt)] = (unsigned short)((ri << 5) | lane);
-      nn += __popc(NEED);
+    if ((P >> lane) & 1u) {
+      const int hx = head_of(Sc, lane);
+      const bool first = (P & lt & ~((1u << hx) - 1u)) == 0u;
+      if (first && ri >= LROW0) par[ri * 32 + hx] = (unsigned short)(nbase[rl] + head_of(Sl, lane));
+      else km |= 2u;
     }
+    const unsigned need = (NEED >> lane) & 1u;
+    const uint32_t Q = __ballot_sync(FULL, (km | need) != 0u);
+    if ((Q >> lane) & 1u) ul[un + __popc(Q & lt)] = (unsigned short)((need << 14) | (km << 11) | (ri << 5) | lane);
+    un += __popc(Q);
   }
-  __syncwarp();
+  __syncthreads();  // every direct link is in place before any union
+
+  // ---- phase 2b: the unions of the warp's own list, one entry per lane.
+  // Bits of a lane's union set: j < NB a needy voxel's relation j; NB the
+  // column x0 - 1 of its row; NB + 1 the row-level pair with the row behind
+  // (6); NB + 2 the row-level pair with the link row.
   int err = 0;
-  // pairs found at row level: lane i takes entry i of each round
-  for (int r0 = 0; r0 < pn; r0 += 32) {
+  for (int r0 = 0; r0 < un; r0 += 32) {
     const int i = r0 + lane;
-    if (i < pn) {
-      const unsigned e = pl[i];
+    if (i < un) {
+      const unsigned e = ul[i];
       const int x = (int)(e & 31u), ri = (int)((e >> 5) & 63u);
+      const unsigned km = (e >> 11) & 7u;
       const int rb = box_row_of(ri);
-      const unsigned short h = (unsigned short)(ri * 32 + head_of(smask[rb], x));
-      unsigned m = PRIMARY ? 1u : (e >> 11);
-      while (m) {
-        const int j = __ffs(m) - 1;
-        m &= m - 1u;
-        unsigned short t;
-        if (j == 2) {
-          t = (unsigned short)(CNODE + rb);
-        } else {
-          const int rbk = rb + (PRIMARY ? POFF : (j == 0 ? -1 : -BY));
-          t = (unsigned short)(nbase[rbk] + head_of(smask[rbk], x));
-        }
-        if (!sunite(par, h, t)) err = 1;
-      }
-    }
-  }
-  // needy voxels: one lane each tests the voxel's remaining relations
-  if constexpr (PRIMARY) {
-    for (int r0 = 0; r0 < nn; r0 += 32) {
-      const int i = r0 + lane;
-      if (i < nn) {
-        const unsigned e = nl[i];
-        const int x = (int)(e & 31u), ri = (int)(e >> 5);
-        const int rb = box_row_of(ri);
+      const uint32_t Sc = smask[rb];
+      const unsigned short h = (unsigned short)(ri * 32 + head_of(Sc, x));
+      uint32_t m = ((km & 4u) ? 1u << NB : 0u) | ((km & 1u) ? 2u << NB : 0u) | ((km & 2u) ? 4u << NB : 0u);
+      if (PRIMARY && ((e >> 14) & 1u)) {
+        // a needy voxel tests its remaining relations itself
         const T v = at(rb, x);
-        const uint32_t Sc = smask[rb];
         const bool head = (Sc >> x) & 1u;
-        const unsigned short h = (unsigned short)(ri * 32 + head_of(Sc, x));
-        uint32_t m = 0;
 #pragma unroll
-        for (int j = 0; j < NRel::n; ++j) {
+        for (int j = 0; j < NB; ++j) {
           const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
           const int k = (int)(c & 3u), dx = (int)(c >> 2) - 1;
           if (((NRel::left >> j) & 1u) && !head) continue;
@@ -337,47 +360,65 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
           if (rel) m |= 1u << j;
         }
         // the column x0 - 1 of the voxel's own row
-        if (x == 0 && R(v, at(rb, -1))) m |= 1u << NRel::n;
-        while (m) {
-          const int j = __ffs(m) - 1;
-          m &= m - 1u;
-          unsigned short t;
-          if (j == NRel::n) {
-            t = (unsigned short)(CNODE + rb);
-          } else {
-            const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
-            const int k = (int)(c & 3u), xn = x + (int)(c >> 2) - 1;
-            const int rbk = rb + (k == 0 ? row_off(0) : (k == 1 ? row_off(1) : (k == 2 ? row_off(2) : row_off(3))));
-            if (xn < 0) t = (unsigned short)(CNODE + rbk);
-            else if (xn > 31) t = (unsigned short)(CNODE + NRB + rbk);
-            else t = (unsigned short)(nbase[rbk] + head_of(smask[rbk], xn));
-          }
-          if (!sunite(par, h, t)) err = 1;
+        if (x == 0 && R(v, at(rb, -1))) m |= 1u << NB;
+      }
+      while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1u;
+        int rbk, xn = x;
+        if (j < NB) {
+          const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
+          const int k = (int)(c & 3u);
+          xn = x + (int)(c >> 2) - 1;
+          rbk = rb + (k == 0 ? row_off(0) : (k == 1 ? row_off(1) : (k == 2 ? row_off(2) : row_off(3))));
+        } else {
+          rbk = j == NB ? rb : (j == NB + 1 ? rb - 1 : rb + LOFF);
+          if (j == NB) xn = -1;
         }
+        unsigned short t;
+        if (xn < 0) t = (unsigned short)(CNODE + rbk);
+        else if (xn > 31) t = (unsigned short)(CNODE + NRB + rbk);
+        else t = (unsigned short)(nbase[rbk] + head_of(smask[rbk], xn));
+        if (!sunite(par, h, t)) err = 1;
       }
     }
   }
   if (err) local_err = 1;
   __syncthreads();
 
-  // ---- phase 3: roots (every head points at its root afterwards), counts
+  // ---- phase 3: roots, run records, keys, bitmap.  A component is named by
+  // its root run (the smallest node of its tree, its first run in raster
+  // order): the run's index in the tile's run order.  Halo heads are only
+  // pointed at their roots, for the edges below.
+  const uint32_t C = rbase[NR];
+  auto rid_of = [&](unsigned r) -> unsigned {
+    return rbase[r >> 5] + __popc(smask[box_row_of((int)(r >> 5))] & ((1u << (r & 31u)) - 1u));
+  };
+  const uint32_t wpr = (uint32_t)g.wpr, word0 = (uint32_t)g.word0, tx = (uint32_t)g.tx;
   for (int rb = warp; rb < NRB; rb += NW) {
     const uint32_t S = smask[rb];
     bool root = false;
+    unsigned short r = 0;
     if ((S >> lane) & 1u) {
       const unsigned short n = (unsigned short)(nbase[rb] + lane);
-      const unsigned short r = sfind_ro(par, n);
+      r = sfind_ro(par, n);
       par[n] = r;
-      root = (r == n);
+      root = r == n;
     }
-    if (is_tile_row(rb)) {
-      const uint32_t rm = __ballot_sync(FULL, root);
-      if (lane == 0) {
-        const int ri = tile_row_of(rb);
-        rootm[ri] = rm;
-        rbase[ri + 1] = (unsigned short)__popc(S);
-        cbase[ri + 1] = (unsigned short)__popc(rm);
-      }
+    if (!(rflag[rb] & 1u)) continue;
+    const int ri = rloc[rb];
+    const uint32_t bw = word0 + rgrow[rb] * wpr + tx;  // bitmap word of the row
+    if ((S >> lane) & 1u) {
+      const unsigned c = rid_of(r);
+      p.rcomp[node0 + rbase[ri] + __popc(S & lt)] = (uint16_t)c;
+      if (root) p.E[node0 + c] = ((unsigned long long)(bw * 32u + (uint32_t)lane) << 32) | (node0 + c);
+    }
+    const uint32_t rm = __ballot_sync(FULL, root);
+    if (lane == 0) {
+      const uint32_t rr = utile * (uint32_t)kRowsPerTile + (uint32_t)ri;
+      p.rmask[rr] = make_uint2(fmask[rb], S);
+      p.rrow[rr] = rbase[ri];
+      if (rflag[rb] & 2u) p.bitmap[bw] = rm;
     }
   }
   for (int c = tid; c < 2 * NRB; c += kThreads) {
@@ -385,114 +426,57 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     par[n] = sfind_ro(par, n);
   }
   __syncthreads();
-  if (warp == 0) {
-    // exclusive prefix over the 64 rows (two per lane)
-    const uint32_t a0 = rbase[2 * lane + 1], a1 = rbase[2 * lane + 2];
-    const uint32_t c0 = cbase[2 * lane + 1], c1 = cbase[2 * lane + 2];
-    uint32_t sa = a0 + a1, sc = c0 + c1;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t ya = __shfl_up_sync(FULL, sa, o), yc = __shfl_up_sync(FULL, sc, o);
-      if (lane >= o) { sa += ya; sc += yc; }
-    }
-    rbase[2 * lane + 1] = (unsigned short)(sa - a1);
-    rbase[2 * lane + 2] = (unsigned short)sa;
-    cbase[2 * lane + 1] = (unsigned short)(sc - c1);
-    cbase[2 * lane + 2] = (unsigned short)sc;
-    if (lane == 0) { rbase[0] = 0; cbase[0] = 0; }
-  }
-  __syncthreads();
-  const uint32_t C = cbase[NR];
-  // dense component id of a root (a tile run head) in tile raster order
-  auto cid_of = [&](unsigned r) -> unsigned {
-    return cbase[r >> 5] + __popc(rootm[r >> 5] & ((1u << (r & 31u)) - 1u));
-  };
 
-  // ---- phase 4: run records, keys, bitmap
-  const uint32_t node0 = (uint32_t)(tile * kTV);
-  for (int ri = warp; ri < NR; ri += NW) {
-    const int rb = box_row_of(ri);
-    const uint32_t S = smask[rb], F = fmask[rb], rm = rootm[ri];
-    const int64_t y = y0 + ri % TY, z = z0 + ri / TY;
-    if (lane == 0) {
-      p.rmask[tile * kRowsPerTile + ri] = make_uint2(F, S);
-      p.rrow[tile * kRowsPerTile + ri] = rbase[ri];
-      if (y < g.sy && z < g.sz) p.bitmap[g.word0 + (z * g.sy + y) * g.wpr + tx] = rm;
-    }
-    if ((S >> lane) & 1u) {
-      const unsigned r = par[ri * 32 + lane];
-      const unsigned c = cid_of(r);
-      p.rcomp[tile * kTV + rbase[ri] + __popc(S & lt)] = (uint16_t)c;
-      if ((rm >> lane) & 1u) {
-        const uint32_t key = (uint32_t)(g.word0 * 32 + (z * g.sy + y) * g.key_row + x0 + lane);
-        p.E[node0 + c] = ((unsigned long long)key << 32) | (node0 + c);
-      }
-    }
-  }
-
-  // ---- one edge per halo run / halo-column voxel joined to a tile component,
-  // except where the same-owner voxel just before it (one row back in y, else
-  // in z) relates to it and joined the same component: both lie in one
-  // component of their own tile, so that edge would repeat
-  auto prev_row = [&](int rb) -> int {
-    const int by = rb % BY, bz = rb / BY, own = row_owner(rb);
-    if (by > 0 && row_owner(rb - 1) == own) return rb - 1;
-    if (bz > 0 && row_owner(rb - BY) == own) return rb - BY;
-    return -1;
-  };
-  auto halo_edge = [&](int h, uint2& e) -> bool {
-    int rb, lx, xi;
-    int64_t gx;
-    unsigned short node;
-    if (h < NRB * 32) {
-      rb = h >> 5;
-      lx = h & 31;
-      if (!((smask[rb] >> lx) & 1u)) return false;  // run heads stand for their runs
-      xi = lx;
-      gx = x0 + lx;
-      node = (unsigned short)(nbase[rb] + lx);
-    } else {
-      const int c = h - NRB * 32;
-      rb = c % NRB;
-      xi = (c < NRB) ? -1 : 32;
-      gx = x0 + xi;
-      lx = (int)(gx & 31);
-      node = (unsigned short)(CNODE + c);
-      if (at(rb, xi) == T(0)) return false;
-    }
-    const unsigned short r = par[node];
-    if (r >= kTV) return false;
-    const int rp = prev_row(rb);
-    if (rp >= 0) {
-      const T a = at(rb, xi), b = at(rp, xi);
-      if (b != T(0) && (MODE == MODE_MULTI ? a == b : true)) {
-        unsigned short np;
-        if (xi < 0) np = (unsigned short)(CNODE + rp);
-        else if (xi > 31) np = (unsigned short)(CNODE + NRB + rp);
-        else np = (unsigned short)(nbase[rp] + head_of(smask[rp], xi));
-        if (par[np] == r) return false;
-      }
-    }
-    const int by = rb % BY, bz = rb / BY;
-    const int64_t gy = y0 - 1 + by, gz = z0 - HZ + bz;
-    const int64_t otile = g.tile0 + (gx >> 5) + (int64_t)g.ntx * ((gy / TY) + (int64_t)g.nty * (gz / TZ));
-    const uint32_t local = (uint32_t)(lx + kTX * ((gy % TY) + TY * (gz % TZ)));
-    e = make_uint2(node0 + cid_of(r), (uint32_t)(otile * kTV + local));
-    return true;
-  };
-  uint2* edges = p.edges + tile * p.edge_slots;
+  // ---- phase 4: one edge per halo run / halo-column voxel joined to a tile
+  // component, except where the same-owner voxel just before it (one row back
+  // in y, else in z) relates to it and joined the same component: both lie
+  // in one component of their own tile, so that edge would repeat
+  uint2* edges = p.edges + (size_t)utile * p.edge_slots;
   constexpr int NCC = (2 * NRB + 31) / 32;  // 32-voxel chunks of the two halo columns
   for (int it = warp; it < NRB + NCC; it += NW) {
-    int h;
+    bool has = false;
+    uint2 e = make_uint2(0u, 0u);
     if (it < NRB) {
-      if (is_tile_row(it)) continue;
-      h = it * 32 + lane;
+      if (rflag[it] & 1u) continue;
+      const int rb = it;
+      if ((smask[rb] >> lane) & 1u) {  // run heads stand for their runs
+        const unsigned short r = par[nbase[rb] + lane];
+        if (r < kTV) {
+          has = true;
+          const int rp = rprev[rb];
+          if (rp != 255) {
+            const T a = at(rb, lane), b = at(rp, lane);
+            if (b != T(0) && (MODE == MODE_MULTI ? a == b : true) &&
+                par[nbase[rp] + head_of(smask[rp], lane)] == r)
+              has = false;
+          }
+          if (has) e = make_uint2(node0 + rid_of(r), (rtile[rb] * (uint32_t)kRowsPerTile + rloc[rb]) * 32u + lane);
+        }
+      }
     } else {
       const int c = (it - NRB) * 32 + lane;
-      h = c < 2 * NRB ? NRB * 32 + c : -1;
+      if (c < 2 * NRB) {
+        const int side = c >= NRB ? 1 : 0, rb = c - side * NRB, xi = side ? 32 : -1;
+        if (at(rb, xi) != T(0)) {
+          const unsigned short r = par[CNODE + c];
+          if (r < kTV) {
+            has = true;
+            const int rp = rprev[rb];
+            if (rp != 255) {
+              const T a = at(rb, xi), b = at(rp, xi);
+              if (b != T(0) && (MODE == MODE_MULTI ? a == b : true) && par[CNODE + side * NRB + rp] == r)
+                has = false;
+            }
+            // the column voxel lies in the tile left (x0 - 1) or right
+            // (x0 + 32) of the row's tile, at x 31 or 0 of that tile
+            if (has)
+              e = make_uint2(node0 + rid_of(r),
+                             ((rtile[rb] + (side ? 1u : 0xFFFFFFFFu)) * (uint32_t)kRowsPerTile + rloc[rb]) * 32u +
+                                 (side ? 0u : 31u));
+          }
+        }
+      }
     }
-    uint2 e;
-    const bool has = h >= 0 && halo_edge(h, e);
     const unsigned m = __ballot_sync(FULL, has);
     if (!m) continue;
     unsigned base = 0;
@@ -530,21 +514,21 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // ---- per-tile results (reduced by the numbering scan, no same-address
   // atomics here)
   if (lane == 0) {
-    auto grow = [&](int rb) -> long long { return (y0 - 1 + rb % BY) + g.sy * (z0 - HZ + rb / BY); };
     red_epl[warp] = epl_acc;
-    red_first[warp] = frb < NRB ? grow(frb) : 0x7FFFFFFFFFFFFFFFLL;
-    red_last[warp] = lrb >= 0 ? grow(lrb) : -1;
+    red_first[warp] = frb;
+    red_last[warp] = lrb;
     red_prov[warp] = prov;
   }
   __syncthreads();
   if (tid == 0) {
     unsigned long long e = 0, pv = 0;
-    long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+    int f = -1, l = -1;
     for (int w = 0; w < NW; ++w) {
       e += red_epl[w];
       pv += red_prov[w];
-      f = red_first[w] < f ? red_first[w] : f;
-      l = red_last[w] > l ? red_last[w] : l;
+      // box-row order is raster order for rows inside the volume
+      if (red_first[w] >= 0 && (f < 0 || red_first[w] < f)) f = red_first[w];
+      if (red_last[w] > l) l = red_last[w];
     }
     const uint32_t nedges = edge_fill;
     TileInfo ti;
@@ -552,8 +536,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     ti.nedges = nedges < p.edge_slots ? nedges : p.edge_slots;
     ti.epl = (uint32_t)e;
     ti.prov = (uint32_t)pv;
-    ti.first_row = f;
-    ti.last_row = l;
+    ti.first_row = f >= 0 ? (long long)rgrow[f] : 0x7FFFFFFFFFFFFFFFLL;
+    ti.last_row = l >= 0 ? (long long)rgrow[l] : -1;
     p.tinfo[tile] = ti;
     if (nedges > p.edge_slots) atomicOr(&p.ctr->err, ERR_EDGE_OVERFLOW);
     if (local_err)

@@ -48,7 +48,7 @@ def test_statistics_rejects_labels_above_n(env):
     the tables.  Its voxels are skipped and the call reports a device error;
     the next call with the right N is exact."""
     cc3d, nat, lib, torch = env
-    lab = torch.arange(64, dtype=torch.uint32, device="cuda").view(4, 4, 4)
+    lab = torch.arange(64, dtype=torch.int32).to(torch.uint32).cuda().view(4, 4, 4)
     N = 10  # the real maximum is 63
     counts = torch.zeros(N + 1, dtype=torch.uint32, device="cuda")
     bbox = torch.zeros((N + 1) * 6, dtype=torch.uint16, device="cuda")
@@ -56,6 +56,6 @@ def test_statistics_rejects_labels_above_n(env):
     rc = lib.cc3d_gpu_statistics(lab.data_ptr(), nat.U32, 4, 4, 4, 3, 1, N, counts.data_ptr(), bbox.data_ptr(),
                                  nat.U16, cent.data_ptr(), nat.IN_DEVICE | nat.OUT_DEVICE, None)
     assert rc == nat.ERR_DEVICE and b"exceeds N" in lib.cc3d_gpu_last_error()
-    assert counts.sum().item() == N + 1  # only labels 0..N were counted
+    assert int(counts.cpu().numpy().astype(np.int64).sum()) == N + 1  # only labels 0..N were counted
     s = cc3d.statistics(lab, no_slice_conversion=True)
     assert s["voxel_counts"].cpu().tolist() == [1] * 64
