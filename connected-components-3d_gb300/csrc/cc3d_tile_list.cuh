@@ -138,6 +138,9 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // per warp: one entry per voxel of its rows that has unions to run:
   // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x
   __shared__ unsigned short ulist[NW][QN];
+  // per warp: union pairs (h << 16) | t waiting for a dense round
+  constexpr int PC = 64;
+  __shared__ uint32_t pairs[NW][PC];
   __shared__ unsigned short rbase[NR + 1];  // first run of every tile row
   __shared__ unsigned long long red_epl[NW];
   __shared__ int red_first[NW], red_last[NW];
@@ -321,21 +324,40 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   }
   __syncthreads();  // every direct link is in place before any union
 
-  // ---- phase 2b: the unions of the warp's own list, one entry per lane.
-  // Bits of a lane's union set: j < NB a needy voxel's relation j; NB the
-  // column x0 - 1 of its row; NB + 1 the row-level pair with the row behind
-  // (6); NB + 2 the row-level pair with the link row.
+  // ---- phase 2b: the warp's list, one entry per lane: its union pairs are
+  // found first (the needy voxels' relation tests), collected, and run in
+  // dense rounds of one union per lane.  Bits of a lane's pair set: j < NB a
+  // needy voxel's relation j; NB the column x0 - 1 of its row; NB + 1 the
+  // row-level pair with the row behind (6); NB + 2 the row-level pair with
+  // the link row.
   int err = 0;
+  int pc = 0;  // warp-uniform pair fill
+  uint32_t* pw = pairs[warp];
+  auto run_pairs = [&]() {
+    __syncwarp();
+    for (int r0 = 0; r0 < pc; r0 += 32) {
+      if (r0 + lane < pc) {
+        const uint32_t q = pw[r0 + lane];
+        if (!sunite(par, (unsigned short)(q >> 16), (unsigned short)(q & 0xFFFFu))) err = 1;
+      }
+    }
+    __syncwarp();
+    pc = 0;
+  };
   for (int r0 = 0; r0 < un; r0 += 32) {
     const int i = r0 + lane;
+    uint32_t m = 0;
+    int x = 0, rb = 0;
+    unsigned short h = 0;
     if (i < un) {
       const unsigned e = ul[i];
-      const int x = (int)(e & 31u), ri = (int)((e >> 5) & 63u);
+      x = (int)(e & 31u);
+      const int ri = (int)((e >> 5) & 63u);
       const unsigned km = (e >> 11) & 7u;
-      const int rb = box_row_of(ri);
+      rb = box_row_of(ri);
       const uint32_t Sc = smask[rb];
-      const unsigned short h = (unsigned short)(ri * 32 + head_of(Sc, x));
-      uint32_t m = ((km & 4u) ? 1u << NB : 0u) | ((km & 1u) ? 2u << NB : 0u) | ((km & 2u) ? 4u << NB : 0u);
+      h = (unsigned short)(ri * 32 + head_of(Sc, x));
+      m = ((km & 4u) ? 1u << NB : 0u) | ((km & 1u) ? 2u << NB : 0u) | ((km & 2u) ? 4u << NB : 0u);
       if (PRIMARY && ((e >> 14) & 1u)) {
         // a needy voxel tests its remaining relations itself
         const T v = at(rb, x);
@@ -344,25 +366,27 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         for (int j = 0; j < NB; ++j) {
           const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
           const int k = (int)(c & 3u), dx = (int)(c >> 2) - 1;
-          if (((NRel::left >> j) & 1u) && !head) continue;
           const int rbk = rb + row_off(k);
-          bool rel = R(v, at(rbk, x + dx));
-          if (dx != 0 && rel) {
+          bool rel = (head || !((NRel::left >> j) & 1u)) && R(v, at(rbk, x + dx));
+          if (dx != 0) {
             // the neighbour run of column x + dx already joined through the
             // dx = 0 relation when it also covers column x
             const int xn = x + dx;
-            if (xn >= 0 && xn <= 31) {
-              const uint32_t Sk = smask[rbk];
-              const bool same = dx > 0 ? !((Sk >> xn) & 1u) : !((Sk >> x) & 1u);
-              if (same && R(v, at(rbk, x))) rel = false;
-            }
+            const uint32_t Sk = smask[rbk];
+            const bool same = (xn >= 0 && xn <= 31) && !((Sk >> (dx > 0 ? xn : x)) & 1u);
+            rel = rel && !(same && R(v, at(rbk, x)));
           }
           if (rel) m |= 1u << j;
         }
         // the column x0 - 1 of the voxel's own row
         if (x == 0 && R(v, at(rb, -1))) m |= 1u << NB;
       }
-      while (m) {
+    }
+    // collect the pairs, one per lane per step
+    while (__any_sync(FULL, m != 0u)) {
+      const uint32_t act = __ballot_sync(FULL, m != 0u);
+      if (pc + __popc(act) > PC) run_pairs();
+      if (m) {
         const int j = __ffs(m) - 1;
         m &= m - 1u;
         int rbk, xn = x;
@@ -379,10 +403,12 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         if (xn < 0) t = (unsigned short)(CNODE + rbk);
         else if (xn > 31) t = (unsigned short)(CNODE + NRB + rbk);
         else t = (unsigned short)(nbase[rbk] + head_of(smask[rbk], xn));
-        if (!sunite(par, h, t)) err = 1;
+        pw[pc + __popc(act & lt)] = ((uint32_t)h << 16) | t;
       }
+      pc += __popc(act);
     }
   }
+  run_pairs();
   if (err) local_err = 1;
   __syncthreads();
 
@@ -433,12 +459,14 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // in one component of their own tile, so that edge would repeat
   uint2* edges = p.edges + (size_t)utile * p.edge_slots;
   constexpr int NCC = (2 * NRB + 31) / 32;  // 32-voxel chunks of the two halo columns
-  for (int it = warp; it < NRB + NCC; it += NW) {
+  for (int it = warp; it < NHR + NCC; it += NW) {
     bool has = false;
     uint2 e = make_uint2(0u, 0u);
-    if (it < NRB) {
-      if (rflag[it] & 1u) continue;
-      const int rb = it;
+    if (it < NHR) {
+      // halo row `it`: the whole first plane in 3D, then the two y faces of
+      // every tile plane
+      const int q = it - HZ * BY;
+      const int rb = q < 0 ? it : (HZ + (q >> 1)) * BY + ((q & 1) ? BY - 1 : 0);
       if ((smask[rb] >> lane) & 1u) {  // run heads stand for their runs
         const unsigned short r = par[nbase[rb] + lane];
         if (r < kTV) {
@@ -454,7 +482,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         }
       }
     } else {
-      const int c = (it - NRB) * 32 + lane;
+      const int c = (it - NHR) * 32 + lane;
       if (c < 2 * NRB) {
         const int side = c >= NRB ? 1 : 0, rb = c - side * NRB, xi = side ? 32 : -1;
         if (at(rb, xi) != T(0)) {
