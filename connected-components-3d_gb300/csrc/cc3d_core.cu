@@ -175,10 +175,12 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
 }
 
 // ---------------------------------------------------------------- resolve
-// Final label of every component: 1 + rank of its root's key among the
-// surviving keys.  A tile's components are named by their root runs (the
-// runs whose component id is their own index).  One warp per tile, one lane
-// per run.
+// Final label of every run: 1 + rank of the key of its component's root
+// among the surviving keys.  A tile's components are named by their root runs
+// (the runs whose component id is their own index): the labels of the root
+// runs are resolved first, then every other run copies its root run's label
+// into its own slot (slots of non-root runs are never read as component
+// labels, so the copy is safe in place).  One warp per tile, one lane per run.
 __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -203,6 +205,13 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
       }
       p.label[node0 + c] = lab;
     }
+    __syncwarp();
+    for (uint32_t c = lane; c < C; c += 32) {
+      const uint32_t r = p.rcomp[node0 + c];
+      if (r == c) continue;
+      if (r < C) p.label[node0 + c] = p.label[node0 + r];
+      else atomicOr(&p.ctr->err, ERR_INDEX);
+    }
   }
 }
 
@@ -212,6 +221,7 @@ cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cu
 
 template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
+  k_resolve<<<152 * 16, 256, 0, s>>>(a);
   return launch_write_tiles_t<OUT>(a, out, ntiles, s);
 }
 
@@ -283,15 +293,15 @@ cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// labels of the tiles [a.tile_base, a.tile_base + count) of a single volume,
-// resolved and written by one block per tile
+// the writer alone (labels resolved), for the tiles [a.tile_base,
+// a.tile_base + count) of a single volume: one block per tile
 template <typename OUT>
 cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  if (a.ty == 8 && a.tz == 8) k_write_fused<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 4 && a.tz == 16) k_write_fused<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 16 && a.tz == 4) k_write_fused<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 64 && a.tz == 1) k_write_fused<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

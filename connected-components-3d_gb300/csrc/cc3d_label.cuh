@@ -37,9 +37,8 @@
 //   k_wrap_pairs  periodic boundaries: unions across wrapped faces.
 //   scan          exclusive popcount prefix of the bitmap: the rank of every
 //                 surviving key = the component's number minus one.
-//   k_write_fused label of each component = 1 + rank(key of its root),
-//                 resolved per tile into shared memory; the run-length records
-//                 expand to the output volume.
+//   k_resolve     label of each run = 1 + rank(key of its component's root)
+//   k_write       the run-length records expand to the output volume.
 //
 // Every loop that waits on other threads (the union-find retries) carries an
 // iteration budget; when it runs out it sets a bit in the device error word
@@ -485,10 +484,10 @@ __device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT
     atomicOr(&p.ctr->err, ERR_INDEX);
     C = kTV;
   }
-  // final labels of the tile's components, resolved by k_resolve.  Each warp
-  // owns 8 rows: the loads of all of them are issued before any store, so a
-  // warp waits for three rounds of loads (run masks and bases, run
-  // components, labels), not three per row.
+  // final labels of the tile's runs, resolved by k_resolve.  Each warp owns
+  // 8 rows: the loads of all of them are issued before any store, so a warp
+  // waits for two rounds of loads (run masks and bases, run labels), not two
+  // per row.
   constexpr int RPW = TY * TZ / (kThreads / 32);
   static_assert(RPW * (kThreads / 32) == TY * TZ, "rows per warp");
   const uint32_t* lab = p.label + tile * kTV;
@@ -502,14 +501,13 @@ __device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT
     m[j] = __ldg(p.rmask + tile * kRowsPerTile + ri);
     run[j] = (int)__ldg(p.rrow + tile * kRowsPerTile + ri);
   }
-  uint32_t c[RPW];
+  uint32_t c[RPW];  // run of every voxel
 #pragma unroll
   for (int j = 0; j < RPW; ++j) {
     c[j] = 0xFFFFFFFFu;
     if ((m[j].x >> lane) & 1u) {
       const int k = __popc(m[j].y & lanemask_le(lane)) - 1;
-      const int r = run[j] + k;
-      c[j] = (k >= 0 && r < kTV) ? (uint32_t)__ldg(p.rcomp + tile * kTV + r) : 0xFFFFFFFEu;
+      c[j] = k >= 0 ? (uint32_t)(run[j] + k) : 0xFFFFFFFEu;
     }
   }
   OUT v[RPW];
@@ -528,70 +526,10 @@ __device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT
   }
 }
 
-// One CTA resolves one tile's component labels and expands its run records
-// into a single volume's output: the label of component c is 1 + the rank of
-// its root's key among the surviving keys (the bitmap prefix), computed once
-// per component into shared memory while the row records and run components
-// are already on their way; then every voxel takes its run's component label.
 template <typename OUT, int TY, int TZ>
 __global__ void __launch_bounds__(kThreads)
-k_write_fused(LabelArgs p, OUT* out) {
-  __shared__ uint32_t lab[kTV];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t tile = p.tile_base + blockIdx.x;
-  const uint32_t ntx = (uint32_t)p.ntx, nty = (uint32_t)p.nty;
-  const uint32_t rest = (uint32_t)tile / ntx, tz = rest / nty;
-  const int64_t x0 = (int64_t)((uint32_t)tile - rest * ntx) * kTX;
-  const int64_t y0 = (int64_t)(rest - tz * nty) * TY, z0 = (int64_t)tz * TZ;
-  constexpr int RPW = TY * TZ / (kThreads / 32);
-  static_assert(RPW * (kThreads / 32) == TY * TZ, "rows per warp");
-  // the row records first: their loads overlap the label resolution below
-  uint2 m[RPW];
-  int run[RPW];
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    const int ri = warp + j * (kThreads / 32);
-    m[j] = __ldg(p.rmask + tile * kRowsPerTile + ri);
-    run[j] = (int)__ldg(p.rrow + tile * kRowsPerTile + ri);
-  }
-  uint32_t c[RPW];
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    c[j] = 0xFFFFFFFFu;
-    if ((m[j].x >> lane) & 1u) {
-      const int k = __popc(m[j].y & lanemask_le(lane)) - 1;
-      const int r = run[j] + k;
-      c[j] = (k >= 0 && r < kTV) ? (uint32_t)__ldg(p.rcomp + tile * kTV + r) : 0xFFFFFFFEu;
-    }
-  }
-  uint32_t C = p.tinfo[tile].C;
-  if (C > kTV) {
-    if (tid == 0) atomicOr(&p.ctr->err, ERR_INDEX);
-    C = kTV;
-  }
-  const uint32_t node0 = (uint32_t)(tile * kTV);
-  for (uint32_t cc = tid; cc < C; cc += kThreads) {
-    if (__ldg(p.rcomp + node0 + cc) != cc) continue;  // only root runs name components
-    const uint32_t R = gfind(p.E, node0 + cc, p.ctr);
-    const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
-    const uint32_t w = key >> 5;
-    uint32_t v = 0;
-    if (w < p.nwords) v = __ldg(p.prefix + w) + __popc(__ldg(p.bitmap + w) & ((1u << (key & 31)) - 1u)) + 1u;
-    else atomicOr(&p.ctr->err, ERR_INDEX);
-    lab[cc] = v;
-  }
-  __syncthreads();
-  const int64_t x = x0 + lane;
-  const bool xin = x < p.sx;
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    OUT v = OUT(0);
-    if (c[j] < C) v = (OUT)lab[c[j]];
-    else if (c[j] != 0xFFFFFFFFu) atomicOr(&p.ctr->err, ERR_INDEX);
-    const int ri = warp + j * (kThreads / 32);
-    const int64_t y = y0 + ri % TY, z = z0 + ri / TY;
-    if (xin && y < p.sy && z < p.sz) out[(z * p.sy + y) * p.sx + x] = v;
-  }
+k_write(LabelArgs p, OUT* out) {
+  write_tile<OUT, TY, TZ>(p, p.tile_base + blockIdx.x, out);
 }
 
 // a batch: every volume has its own output buffer and element type

@@ -300,7 +300,10 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     const uint32_t P = M & (Sc | Sl | ~(M << 1));
     uint32_t NEED = 0, km = 0;
     if constexpr (CONN == 26 || CONN == 8) {
-      NEED = F & ~M;
+      // a needy voxel that continues a run whose next voxel relates to its
+      // primary neighbour needs nothing: it only has dx = +1 relations of its
+      // own, and each of them is that next voxel's dx = 0 relation, implied
+      NEED = F & ~M & ~(~Sc & (M >> 1) & ~(Sc >> 1) & 0x7FFFFFFFu);
     } else if constexpr (CONN == 18) {
       NEED = F & ~(M & __ballot_sync(FULL, fg && R(v, at(rb - 1, lane))));
     } else {
