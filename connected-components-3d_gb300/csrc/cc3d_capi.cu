@@ -668,7 +668,6 @@ int cc3d_gpu_label_finish(uint64_t token, int64_t max_labels, void* out, int out
   if (nchunks > 1) {
     // labels leave chunk by chunk on the copy stream while the writer
     // produces the next chunk
-    CK(launch_resolve(job.args, s));
     for (int k = 0; k < nchunks; ++k) {
       int64_t t0, t1, v0, v1;
       chunk_range(job.args, k, nchunks, t0, t1, v0, v1);

@@ -53,22 +53,60 @@ constexpr int64_t kScanChunk = (int64_t)kScanThreads * kScanPer;
 
 int64_t scan_blocks_needed(int64_t nwords) { return (nwords + kScanChunk - 1) / kScanChunk; }
 
+// Per-block popcount sums of the bitmap; each block also reduces its share
+// of the tile pass's per-tile results (estimate, provisional count, edges,
+// first/last row) into the counters.
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t* bitmap, int64_t nwords,
-                                                              uint32_t* bsum) {
+                                                              uint32_t* bsum, const TileInfo* ti,
+                                                              int64_t ntiles, Counters* ctr) {
   const int64_t base = blockIdx.x * kScanChunk;
   uint32_t s = 0;
   for (int k = 0; k < kScanPer; ++k) {
     const int64_t w = base + (int64_t)k * kScanThreads + threadIdx.x;
     if (w < nwords) s += __popc(bitmap[w]);
   }
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
+  unsigned long long epl = 0, prov = 0, edges = 0;
+  long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
+  const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int64_t t0 = blockIdx.x * per, t1 = t0 + per < ntiles ? t0 + per : ntiles;
+  for (int64_t t = t0 + threadIdx.x; t < t1; t += kScanThreads) {
+    const TileInfo x = ti[t];
+    epl += x.epl;
+    prov += x.prov;
+    edges += x.nedges;
+    f = x.first_row < f ? x.first_row : f;
+    l = x.last_row > l ? x.last_row : l;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(FULL, s, o);
+    epl += __shfl_down_sync(FULL, epl, o);
+    prov += __shfl_down_sync(FULL, prov, o);
+    edges += __shfl_down_sync(FULL, edges, o);
+    f = min(f, (long long)__shfl_down_sync(FULL, f, o));
+    l = max(l, (long long)__shfl_down_sync(FULL, l, o));
+  }
   __shared__ uint32_t ws[kScanThreads / 32];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __shared__ unsigned long long we[kScanThreads / 32], wp[kScanThreads / 32], wd[kScanThreads / 32];
+  __shared__ long long wf[kScanThreads / 32], wl[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { ws[warp] = s; we[warp] = epl; wp[warp] = prov; wd[warp] = edges; wf[warp] = f; wl[warp] = l; }
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t t = 0;
-    for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      t += ws[w];
+      if (w) {
+        epl += we[w]; prov += wp[w]; edges += wd[w];
+        f = wf[w] < f ? wf[w] : f;
+        l = wl[w] > l ? wl[w] : l;
+      }
+    }
     bsum[blockIdx.x] = t;
+    if (epl) atomicAdd(&ctr->epl, epl);
+    if (prov) atomicAdd(&ctr->prov, prov);
+    if (edges) atomicAdd(&ctr->edges, (unsigned)edges);
+    if (f != 0x7FFFFFFFFFFFFFFFLL) atomicMin(&ctr->first_row, f);
+    if (l >= 0) atomicMax(&ctr->last_row, l);
   }
 }
 
@@ -104,44 +142,6 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t* bsum, int64_t nb
   if (threadIdx.x == 0) ctr->N = carry;
 }
 
-// reduction of the tile pass's per-tile results (one block)
-__global__ void __launch_bounds__(1024) k_reduce_tiles(const TileInfo* ti, int64_t ntiles, Counters* ctr) {
-  unsigned long long epl = 0, prov = 0, edges = 0;
-  long long f = 0x7FFFFFFFFFFFFFFFLL, l = -1;
-  for (int64_t t = threadIdx.x; t < ntiles; t += blockDim.x) {
-    const TileInfo x = ti[t];
-    epl += x.epl;
-    prov += x.prov;
-    edges += x.nedges;
-    f = x.first_row < f ? x.first_row : f;
-    l = x.last_row > l ? x.last_row : l;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    epl += __shfl_down_sync(FULL, epl, o);
-    prov += __shfl_down_sync(FULL, prov, o);
-    edges += __shfl_down_sync(FULL, edges, o);
-    f = min(f, (long long)__shfl_down_sync(FULL, f, o));
-    l = max(l, (long long)__shfl_down_sync(FULL, l, o));
-  }
-  __shared__ unsigned long long se[32], sp[32], sd[32];
-  __shared__ long long sf[32], sl[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) { se[warp] = epl; sp[warp] = prov; sd[warp] = edges; sf[warp] = f; sl[warp] = l; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-      epl += se[w]; prov += sp[w]; edges += sd[w];
-      f = sf[w] < f ? sf[w] : f;
-      l = sl[w] > l ? sl[w] : l;
-    }
-    ctr->epl = epl;
-    ctr->prov = prov;
-    ctr->edges = (unsigned)(edges > 0xFFFFFFFFull ? 0xFFFFFFFFull : edges);
-    ctr->first_row = f;
-    ctr->last_row = l;
-  }
-}
-
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(const uint32_t* bitmap, int64_t nwords,
                                                             const uint32_t* bsum, uint32_t* prefix) {
   __shared__ uint32_t ws[kScanThreads / 32];
@@ -167,9 +167,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const uint32_t* bitm
 cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int64_t nblocks,
                         cudaStream_t s) {
   if (nblocks == 0) return cudaSuccess;
-  k_scan_reduce<<<(unsigned)nblocks, kScanThreads, 0, s>>>(a.bitmap, nwords, bsum);
+  k_scan_reduce<<<(unsigned)nblocks, kScanThreads, 0, s>>>(a.bitmap, nwords, bsum, a.tinfo, a.ntiles, a.ctr);
   k_scan_blocks<<<1, 1024, 0, s>>>(bsum, nblocks, a.ctr);
-  k_reduce_tiles<<<1, 1024, 0, s>>>(a.tinfo, a.ntiles, a.ctr);
   k_scan_down<<<(unsigned)nblocks, kScanThreads, 0, s>>>(a.bitmap, nwords, bsum, a.prefix);
   return cudaGetLastError();
 }
@@ -180,19 +179,29 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
 // (the runs whose component id is their own index): the labels of the root
 // runs are resolved first, then every other run copies its root run's label
 // into its own slot (slots of non-root runs are never read as component
-// labels, so the copy is safe in place).  One warp per tile, one lane per run.
-__global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
+// labels, so the copy is safe in place).  One warp per tile; each lane takes
+// 8 runs at a time with all their loads in flight together.
+__global__ void __launch_bounds__(256) k_resolve(LabelArgs p, int64_t ntiles) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < p.ntiles;
-       tile += warps) {
-    uint32_t C = p.tinfo[tile].C;
-    if (C > kTV) C = kTV;
-    const uint32_t node0 = (uint32_t)(tile * kTV);
-    // a batch numbers each volume from 1: subtract the keys of the volumes before it
-    const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
-    for (uint32_t c = lane; c < C; c += 32) {
-      if (p.rcomp[node0 + c] != c) continue;  // not a root run: no entry of its own
+  const int64_t tile = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (tile >= ntiles) return;
+  uint32_t C = p.tinfo[tile].C;
+  if (C > kTV) C = kTV;
+  const uint32_t node0 = (uint32_t)(tile * kTV);
+  // a batch numbers each volume from 1: subtract the keys of the volumes before it
+  const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
+  constexpr int PER = 8;
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (rc[k] != c) continue;  // not a root run: no entry of its own
       const uint32_t R = gfind(p.E, node0 + c, p.ctr);
       const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
       const uint32_t w = key >> 5;
@@ -205,14 +214,32 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p) {
       }
       p.label[node0 + c] = lab;
     }
-    __syncwarp();
-    for (uint32_t c = lane; c < C; c += 32) {
-      const uint32_t r = p.rcomp[node0 + c];
-      if (r == c) continue;
-      if (r < C) p.label[node0 + c] = p.label[node0 + r];
+  }
+  __syncwarp();
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER], lab[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : c;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      lab[k] = (c < C && rc[k] != c && rc[k] < C) ? p.label[node0 + rc[k]] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (c >= C || rc[k] == c) continue;
+      if (rc[k] < C) p.label[node0 + c] = lab[k];
       else atomicOr(&p.ctr->err, ERR_INDEX);
     }
   }
+}
+
+static void launch_resolve_all(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  if (ntiles > 0) k_resolve<<<(unsigned)((ntiles + 7) / 8), 256, 0, s>>>(a, ntiles);
 }
 
 // ---------------------------------------------------------------- writer
@@ -221,7 +248,6 @@ cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cu
 
 template <typename OUT>
 cudaError_t launch_write_t(const LabelArgs& a, OUT* out, int64_t ntiles, cudaStream_t s) {
-  k_resolve<<<152 * 16, 256, 0, s>>>(a);
   return launch_write_tiles_t<OUT>(a, out, ntiles, s);
 }
 
@@ -279,7 +305,7 @@ cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, 
 }
 
 cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  k_resolve<<<152 * 16, 256, 0, s>>>(a);
+  launch_resolve_all(a, ntiles, s);
   if (a.ty == 8 && a.tz == 8) k_write_batch<8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   else if (a.ty == 4 && a.tz == 16) k_write_batch<4, 16><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
   else if (a.ty == 16 && a.tz == 4) k_write_batch<16, 4><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
@@ -289,19 +315,21 @@ cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t 
 }
 
 cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
-  k_resolve<<<152 * 16, 256, 0, s>>>(a);
+  launch_resolve_all(a, a.ntiles, s);
   return cudaGetLastError();
 }
 
-// the writer alone (labels resolved), for the tiles [a.tile_base,
-// a.tile_base + count) of a single volume: one block per tile
+// labels of the tiles [a.tile_base, a.tile_base + count) of a single volume,
+// resolved and written by one warp per tile
 template <typename OUT>
 cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  if (a.ty == 8 && a.tz == 8) k_write<OUT, 8, 8><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 4 && a.tz == 16) k_write<OUT, 4, 16><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 16 && a.tz == 4) k_write<OUT, 16, 4><<<(unsigned)count, kThreads, 0, s>>>(a, out);
-  else if (a.ty == 64 && a.tz == 1) k_write<OUT, 64, 1><<<(unsigned)count, kThreads, 0, s>>>(a, out);
+  const unsigned blocks = (unsigned)((count + kLabelWarps - 1) / kLabelWarps);
+  constexpr int NT = kLabelWarps * 32;
+  if (a.ty == 8 && a.tz == 8) k_label_write<OUT, 8, 8><<<blocks, NT, 0, s>>>(a, out, count);
+  else if (a.ty == 4 && a.tz == 16) k_label_write<OUT, 4, 16><<<blocks, NT, 0, s>>>(a, out, count);
+  else if (a.ty == 16 && a.tz == 4) k_label_write<OUT, 16, 4><<<blocks, NT, 0, s>>>(a, out, count);
+  else if (a.ty == 64 && a.tz == 1) k_label_write<OUT, 64, 1><<<blocks, NT, 0, s>>>(a, out, count);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

@@ -532,6 +532,121 @@ k_write(LabelArgs p, OUT* out) {
   write_tile<OUT, TY, TZ>(p, p.tile_base + blockIdx.x, out);
 }
 
+// Label resolution and label writing of a single volume, one warp per tile:
+// the labels of the tile's root runs (1 + rank of their root's key among the
+// surviving keys), then every run's label (a non-root run copies its root
+// run's), then the tile's 64 rows.  Up to 256 runs keep their labels in the
+// warp's shared-memory table; a tile with more runs keeps them in the global
+// per-run label slots.  With a warp (not a block) per tile, 64 tiles per SM
+// have their dependent loads in flight at once.
+constexpr int kLabelWarps = 4;
+template <typename OUT, int TY, int TZ>
+__global__ void __launch_bounds__(kLabelWarps * 32)
+k_label_write(LabelArgs p, OUT* out, int64_t count) {
+  __shared__ uint32_t slab[kLabelWarps][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * kLabelWarps + w;
+  if (t >= count) return;
+  const int64_t tile = p.tile_base + t;
+  uint32_t* lab = slab[w];
+  const uint32_t ntx = (uint32_t)p.ntx, nty = (uint32_t)p.nty;
+  const uint32_t rest = (uint32_t)tile / ntx, tz = rest / nty;
+  const int64_t x0 = (int64_t)((uint32_t)tile - rest * ntx) * kTX;
+  const int64_t y0 = (int64_t)(rest - tz * nty) * TY, z0 = (int64_t)tz * TZ;
+  uint32_t C = p.tinfo[tile].C;
+  if (C > kTV) {
+    if (lane == 0) atomicOr(&p.ctr->err, ERR_INDEX);
+    C = kTV;
+  }
+  const uint32_t node0 = (uint32_t)(tile * kTV);
+  // row records of rows lane and lane + 32, fetched while the labels resolve
+  const uint2 ma = __ldg(p.rmask + tile * kRowsPerTile + lane), mb = __ldg(p.rmask + tile * kRowsPerTile + 32 + lane);
+  const uint32_t ra = __ldg(p.rrow + tile * kRowsPerTile + lane), rb = __ldg(p.rrow + tile * kRowsPerTile + 32 + lane);
+  auto root_label = [&](uint32_t c) -> uint32_t {
+    const uint32_t R = gfind(p.E, node0 + c, p.ctr);
+    const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
+    const uint32_t wd = key >> 5;
+    if (wd >= p.nwords) {
+      atomicOr(&p.ctr->err, ERR_INDEX);
+      return 0u;
+    }
+    return __ldg(p.prefix + wd) + __popc(__ldg(p.bitmap + wd) & ((1u << (key & 31)) - 1u)) + 1u;
+  };
+  const bool fast = C <= 256;
+  uint32_t* glab = p.label + node0;
+  constexpr int PER = 8;
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)__ldg(p.rcomp + node0 + c) : 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (rc[k] != c) continue;  // only root runs name components
+      const uint32_t v = root_label(c);
+      if (fast) lab[c] = v;
+      else glab[c] = v;
+    }
+  }
+  __syncwarp();
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER], v[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)__ldg(p.rcomp + node0 + c) : c;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      v[k] = 0u;
+      if (c < C && rc[k] != c) {
+        if (rc[k] < C) v[k] = fast ? lab[rc[k]] : glab[rc[k]];
+        else atomicOr(&p.ctr->err, ERR_INDEX);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (c < C && rc[k] != c) {
+        if (fast) lab[c] = v[k];
+        else glab[c] = v[k];
+      }
+    }
+  }
+  __syncwarp();
+  const int64_t x = x0 + lane;
+  const bool xin = x < p.sx;
+  constexpr int RB = 8;  // rows per batch: their label loads are in flight together
+#pragma unroll 1
+  for (int r0 = 0; r0 < kRowsPerTile; r0 += RB) {
+    OUT v[RB];
+#pragma unroll
+    for (int j = 0; j < RB; ++j) {
+      const int ri = r0 + j;
+      const uint32_t F = __shfl_sync(FULL, ri < 32 ? ma.x : mb.x, ri & 31);
+      const uint32_t S = __shfl_sync(FULL, ri < 32 ? ma.y : mb.y, ri & 31);
+      const uint32_t b = __shfl_sync(FULL, ri < 32 ? ra : rb, ri & 31);
+      v[j] = OUT(0);
+      if ((F >> lane) & 1u) {
+        const int k = __popc(S & lanemask_le(lane)) - 1;
+        const uint32_t r = b + (uint32_t)k;
+        if (k >= 0 && r < C) v[j] = (OUT)(fast ? lab[r] : glab[r]);
+        else atomicOr(&p.ctr->err, ERR_INDEX);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < RB; ++j) {
+      const int ri = r0 + j;
+      const int64_t y = y0 + ri % TY, z = z0 + ri / TY;
+      if (xin && y < p.sy && z < p.sz) out[(z * p.sy + y) * p.sx + x] = v[j];
+    }
+  }
+}
+
 // a batch: every volume has its own output buffer and element type
 template <int TY, int TZ>
 __global__ void __launch_bounds__(kThreads)

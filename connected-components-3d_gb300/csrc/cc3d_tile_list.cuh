@@ -43,6 +43,8 @@
 // provisional count, per-tile results.
 #pragma once
 
+#include <type_traits>
+
 #include "cc3d_tile.cuh"
 
 namespace cc3dgpu {
@@ -92,6 +94,44 @@ template <> struct NeedRels<4> {
   static constexpr unsigned left = 0;
 };
 
+// Union-find over parent words in shared memory: 32-bit words (a native
+// shared-memory CAS) where the tile fits the static shared-memory budget with
+// them, else 16-bit words (8-byte elements).  A root is linked under the
+// smaller root, so the root of every tree is its smallest node.  Every loop
+// is bounded.
+template <typename PT>
+static __device__ __forceinline__ uint32_t lfind(volatile PT* par, uint32_t n) {
+  for (int it = 0; it < kLocalLimit; ++it) {
+    const uint32_t p = par[n];
+    if (p == n) return n;
+    const uint32_t g = par[p];
+    if (g != p) par[n] = (PT)g;  // path halving
+    n = g;
+  }
+  return n;
+}
+template <typename PT>
+static __device__ __forceinline__ uint32_t lfind_ro(const volatile PT* par, uint32_t n) {
+  for (int it = 0; it < kLocalLimit; ++it) {
+    const uint32_t p = par[n];
+    if (p == n) return n;
+    n = p;
+  }
+  return n;
+}
+template <typename PT>
+static __device__ __forceinline__ bool lunite(PT* par, uint32_t a, uint32_t b) {
+  volatile PT* vp = par;
+  for (int it = 0; it < kLocalLimit; ++it) {
+    a = lfind<PT>(vp, a);
+    b = lfind<PT>(vp, b);
+    if (a == b) return true;
+    if (a < b) { const uint32_t t = a; a = b; b = t; }
+    if ((uint32_t)atomicCAS(par + a, (PT)a, (PT)b) == a) return true;
+  }
+  return false;
+}
+
 template <typename T, int CONN, int TY, int TZ, int MODE>
 __global__ void __launch_bounds__(kThreads, 6)
 k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
@@ -127,7 +167,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __shared__ __align__(128) T box[NRB * W];
   __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t smask[NRB], fmask[NRB];
-  __shared__ __align__(16) unsigned short par[NODES];
+  using PT = typename std::conditional<sizeof(T) == 8, unsigned short, uint32_t>::type;
+  __shared__ __align__(16) PT par[NODES];
   // per box row: node id of its voxel 0; the tile holding its 32 voxels and
   // the row's index inside that tile; the same-owner box row before it (one
   // back in y, else in z; 255: none); global row index y + sy * z; flags
@@ -231,8 +272,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     rgrow[rb] = in_vol ? (uint32_t)(y + g.sy * z) : 0u;
     rprev[rb] = (unsigned char)prev;
     rflag[rb] = (unsigned char)((trow ? 1 : 0) | (in_vol ? 2 : 0));
-    par[CNODE + rb] = (unsigned short)(CNODE + rb);
-    par[CNODE + NRB + rb] = (unsigned short)(CNODE + NRB + rb);
+    par[CNODE + rb] = (PT)(CNODE + rb);
+    par[CNODE + NRB + rb] = (PT)(CNODE + NRB + rb);
   }
   if (use_tma) {
     __syncthreads();  // the barrier is initialised before anyone polls it
@@ -260,8 +301,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       smask[rb] = S;
     }
     if ((S >> lane) & 1u) {
-      const unsigned short n = (unsigned short)(nbase[rb] + lane);
-      par[n] = n;
+      const uint32_t n = nbase[rb] + lane;
+      par[n] = (PT)n;
     }
     if (MODE == MODE_MULTI && E && (rflag[rb] & 1u)) {
       epl_acc += __popc(E);
@@ -317,7 +358,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     if ((P >> lane) & 1u) {
       const int hx = head_of(Sc, lane);
       const bool first = (P & lt & ~((1u << hx) - 1u)) == 0u;
-      if (first && ri >= LROW0) par[ri * 32 + hx] = (unsigned short)(nbase[rl] + head_of(Sl, lane));
+      if (first && ri >= LROW0) par[ri * 32 + hx] = (PT)(nbase[rl] + head_of(Sl, lane));
       else km |= 2u;
     }
     const unsigned need = (NEED >> lane) & 1u;
@@ -341,7 +382,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     for (int r0 = 0; r0 < pc; r0 += 32) {
       if (r0 + lane < pc) {
         const uint32_t q = pw[r0 + lane];
-        if (!sunite(par, (unsigned short)(q >> 16), (unsigned short)(q & 0xFFFFu))) err = 1;
+        if (!lunite<PT>(par, q >> 16, q & 0xFFFFu)) err = 1;
       }
     }
     __syncwarp();
@@ -427,11 +468,11 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   for (int rb = warp; rb < NRB; rb += NW) {
     const uint32_t S = smask[rb];
     bool root = false;
-    unsigned short r = 0;
+    uint32_t r = 0;
     if ((S >> lane) & 1u) {
-      const unsigned short n = (unsigned short)(nbase[rb] + lane);
-      r = sfind_ro(par, n);
-      par[n] = r;
+      const uint32_t n = nbase[rb] + lane;
+      r = lfind_ro<PT>(par, n);
+      par[n] = (PT)r;
       root = r == n;
     }
     if (!(rflag[rb] & 1u)) continue;
@@ -451,8 +492,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     }
   }
   for (int c = tid; c < 2 * NRB; c += kThreads) {
-    const unsigned short n = (unsigned short)(CNODE + c);
-    par[n] = sfind_ro(par, n);
+    const uint32_t n = (uint32_t)(CNODE + c);
+    par[n] = (PT)lfind_ro<PT>(par, n);
   }
   __syncthreads();
 
@@ -471,7 +512,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       const int q = it - HZ * BY;
       const int rb = q < 0 ? it : (HZ + (q >> 1)) * BY + ((q & 1) ? BY - 1 : 0);
       if ((smask[rb] >> lane) & 1u) {  // run heads stand for their runs
-        const unsigned short r = par[nbase[rb] + lane];
+        const uint32_t r = par[nbase[rb] + lane];
         if (r < kTV) {
           has = true;
           const int rp = rprev[rb];
@@ -489,7 +530,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       if (c < 2 * NRB) {
         const int side = c >= NRB ? 1 : 0, rb = c - side * NRB, xi = side ? 32 : -1;
         if (at(rb, xi) != T(0)) {
-          const unsigned short r = par[CNODE + c];
+          const uint32_t r = par[CNODE + c];
           if (r < kTV) {
             has = true;
             const int rp = rprev[rb];
