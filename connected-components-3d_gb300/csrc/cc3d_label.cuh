@@ -618,31 +618,51 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
     }
   }
   __syncwarp();
-  const int64_t x = x0 + lane;
-  const bool xin = x < p.sx;
-  constexpr int RB = 8;  // rows per batch: their label loads are in flight together
-#pragma unroll 1
-  for (int r0 = 0; r0 < kRowsPerTile; r0 += RB) {
-    OUT v[RB];
+  // the rows, four per step: lane = 8 * (row of the four) + group; a lane
+  // writes the 4 consecutive voxels 4 * group .. 4 * group + 3 of its row
+  // with one vector store where the output allows it
+  const int g4 = (lane & 7) * 4, rq = lane >> 3;
+  const int64_t xg = x0 + g4;
+  const bool vec = ((p.sx & 3) == 0) && ((reinterpret_cast<uintptr_t>(out) & (4 * sizeof(OUT) - 1)) == 0) &&
+                   (sizeof(OUT) <= 4 || (reinterpret_cast<uintptr_t>(out) & 15) == 0);
+  const int64_t plane = p.sx * p.sy;
+  OUT* base_ptr = out + z0 * plane + y0 * p.sx + xg;
+#pragma unroll 2
+  for (int r0 = 0; r0 < kRowsPerTile; r0 += 4) {
+    const int ri = r0 + rq;
+    const uint32_t F = __shfl_sync(FULL, r0 < 32 ? ma.x : mb.x, ri & 31);
+    const uint32_t S = __shfl_sync(FULL, r0 < 32 ? ma.y : mb.y, ri & 31);
+    const uint32_t b = __shfl_sync(FULL, r0 < 32 ? ra : rb, ri & 31);
+    OUT v[4];
+    // run of voxel g4 (the last run start at or before it), then of the next three
+    int k = __popc(S & lanemask_le(g4)) - 1;
 #pragma unroll
-    for (int j = 0; j < RB; ++j) {
-      const int ri = r0 + j;
-      const uint32_t F = __shfl_sync(FULL, ri < 32 ? ma.x : mb.x, ri & 31);
-      const uint32_t S = __shfl_sync(FULL, ri < 32 ? ma.y : mb.y, ri & 31);
-      const uint32_t b = __shfl_sync(FULL, ri < 32 ? ra : rb, ri & 31);
-      v[j] = OUT(0);
-      if ((F >> lane) & 1u) {
-        const int k = __popc(S & lanemask_le(lane)) - 1;
+    for (int i = 0; i < 4; ++i) {
+      if (i) k += (S >> (g4 + i)) & 1u;
+      v[i] = OUT(0);
+      if ((F >> (g4 + i)) & 1u) {
         const uint32_t r = b + (uint32_t)k;
-        if (k >= 0 && r < C) v[j] = (OUT)(fast ? lab[r] : glab[r]);
+        if (k >= 0 && r < C) v[i] = (OUT)(fast ? lab[r] : glab[r]);
         else atomicOr(&p.ctr->err, ERR_INDEX);
       }
     }
+    const int ly = ri % TY, lz = ri / TY;
+    if (y0 + ly >= p.sy || z0 + lz >= p.sz) continue;
+    OUT* dst = base_ptr + lz * plane + ly * p.sx;
+    if (vec && xg + 3 < p.sx) {
+      if constexpr (sizeof(OUT) == 2) {
+        *reinterpret_cast<uint2*>(dst) = make_uint2((uint32_t)v[0] | ((uint32_t)v[1] << 16),
+                                                    (uint32_t)v[2] | ((uint32_t)v[3] << 16));
+      } else if constexpr (sizeof(OUT) == 4) {
+        *reinterpret_cast<uint4*>(dst) = make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3]);
+      } else {
+        *reinterpret_cast<ulonglong2*>(dst) = make_ulonglong2((unsigned long long)v[0], (unsigned long long)v[1]);
+        *reinterpret_cast<ulonglong2*>(dst + 2) = make_ulonglong2((unsigned long long)v[2], (unsigned long long)v[3]);
+      }
+    } else {
 #pragma unroll
-    for (int j = 0; j < RB; ++j) {
-      const int ri = r0 + j;
-      const int64_t y = y0 + ri % TY, z = z0 + ri / TY;
-      if (xin && y < p.sy && z < p.sz) out[(z * p.sy + y) * p.sx + x] = v[j];
+      for (int i = 0; i < 4; ++i)
+        if (xg + i < p.sx) dst[i] = v[i];
     }
   }
 }
