@@ -442,6 +442,11 @@ def run_gpu(args, world, rank, local):
     if world == 1 and not args.skip_cpu:
         cpu = cpu_reference(vol)
 
+    # the mixed-size stream: batched vs the plain per-volume path
+    batch = None
+    if world == 1 and not args.skip_batch:
+        batch = measure_batch(batch_stream(BATCH_VOLUMES), max(3, min(args.steps, 10)), 3)
+
     launches_per_step = 8  # tile pass, edge merge, 3 scan kernels + tile reduction, resolve, write
     line = {
         "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": world,
@@ -473,6 +478,7 @@ def run_gpu(args, world, rank, local):
                               "frac": pipeline_gbs / peak, "frac_of_spec": pipeline_gbs / HBM_SPEC_GBS,
                               "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items() if v[1]}},
         "cpu_baseline": cpu,
+        "batch": batch,
         "clocks": clocks,
         "gpu_launches": launches_per_step * args.steps,
         "host_wall_s": t_host,
@@ -688,47 +694,118 @@ def cpu_stream_all_cores(vols, kind: str, reps: int = 3):
                       f"processes, largest first; median of {reps} passes ({t:.3f} s per pass)"}
 
 
-def run_batch(args):
-    """The mixed-size stream: N uint16 Voronoi+membrane volumes, every edge
-    log-uniform in [16, 256], one seed per 4096 voxels, labels in [1, 65535],
-    26-connectivity.  One JSON line: the batched path (one launch per stage,
-    replayed CUDA graph, tile pass from the batch autotuner) against one
-    connected_components call per volume, the reference's CPU path on one
-    core (a bounded sample) and on every host core (the whole stream).  Every
-    batched volume is checked against its single-volume result."""
+BATCH_VOLUMES = 1024  # the mixed-size stream of the default line
+
+
+def batch_stream(n: int):
+    """The mixed-size stream: n uint16 Voronoi+membrane volumes, every edge
+    log-uniform in [16, 256], one seed per 4096 voxels, labels in [1, 65535]."""
+    from cc3d_gb300 import synth
+    shapes = synth.batch_shapes(n, 16, 256, seed=12)
+    return [synth.voronoi_volume(s, max(1, int(np.prod(s)) // 4096), 65535, seed=100 + i, dtype=np.uint16,
+                                 salt=0.0) for i, s in enumerate(shapes)]
+
+
+def measure_batch(vols, steps: int, warmup: int) -> dict:
+    """The batched path against the plain per-volume path on the same stream,
+    26-connectivity, device-resident inputs.
+
+    batched   cc3d.connected_components_batch, tile pass from the batch
+              autotuner; every timed step labels the stream in a fresh
+              random order, so each step is a new batch layout and its CUDA
+              graph is captured inside the timed region.
+    per volume  one cc3d_gpu_label_prepare + cc3d_gpu_label_finish per volume
+              through the C ABI (ctypes, device buffers, outputs allocated
+              beforehand), one tile-pass configuration (list/8x8) for all.
+    Every volume's batched labels, N and dtype are checked against its
+    per-volume result."""
     import torch
     import cc3d_gb300 as cc3d
-    from cc3d_gb300 import synth
-    cc3d.build()
-    shapes = synth.batch_shapes(args.batch, 16, 256, seed=12)
-    t0 = time.perf_counter()
-    vols = [synth.voronoi_volume(s, max(1, int(np.prod(s)) // 4096), 65535, seed=100 + i, dtype=np.uint16,
-                                 salt=0.0) for i, s in enumerate(shapes)]
-    t_gen = time.perf_counter() - t0
+    nat = cc3d._native
+    lib = nat.load()
     voxels = int(sum(v.size for v in vols))
     dev = [torch.from_numpy(v).cuda() for v in vols]
     tuned = cc3d.autotune_batch(dev, connectivity=26)
+    rng = np.random.default_rng(5)
 
-    def timed(fn, steps):
-        for _ in range(args.warmup):
+    def batched():
+        order = rng.permutation(len(dev))
+        return cc3d.connected_components_batch([dev[i] for i in order], connectivity=26, return_N=True)
+
+    def timed(fn, k):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
+        t0 = time.perf_counter()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        for _ in range(steps):
+        for _ in range(k):
             fn()
         e1.record()
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / steps
+        return max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3) / k
 
-    ms_batch = timed(lambda: cc3d.connected_components_batch(dev, connectivity=26), args.steps)
-    ms_loop = timed(lambda: [cc3d.connected_components(d, connectivity=26) for d in dev], max(1, args.steps // 3))
-    # every volume: batched == single-volume path
+    ms_batch = timed(batched, steps)
+    # the plain path: per-volume C ABI calls, preallocated uint32 outputs
+    outs = [torch.empty(d.shape, dtype=torch.uint32, device="cuda") for d in dev]
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    flags = nat.IN_DEVICE | nat.OUT_DEVICE
+    prev = cc3d.set_tile_pass("list/8x8")
+
+    def plain():
+        res = []
+        for d, o in zip(dev, outs):
+            sz, sy, sx = d.shape
+            info = nat.Prepared()
+            nat.check(lib.cc3d_gpu_label_prepare(d.data_ptr(), nat.U16, sx, sy, sz, 26, 0, 0, flags, stream,
+                                                 ctypes.byref(info)))
+            n = ctypes.c_uint64(0)
+            code = nat.U16 if min(info.epl, d.numel()) < 65535 else nat.U32
+            nat.check(lib.cc3d_gpu_label_finish(info.token, int(min(info.epl, d.numel())), o.data_ptr(), code,
+                                                ctypes.byref(n), flags, stream))
+            res.append((n.value, code))
+        return res
+
+    try:
+        ms_plain = timed(plain, max(1, steps // 2))
+        plain_res = plain()
+    finally:
+        cc3d.set_tile_pass(prev)
     got = cc3d.connected_components_batch(dev, connectivity=26, return_N=True)
     mismatches = 0
-    for d, (lab, n) in zip(dev, got):
-        ref, rn = cc3d.connected_components(d, connectivity=26, return_N=True)
-        mismatches += int(rn != n or ref.dtype != lab.dtype or not torch.equal(ref.to(torch.int64), lab.to(torch.int64)))
+    for (lab, n), (pn, pcode), o in zip(got, plain_res, outs):
+        pdt = torch.uint16 if pcode == nat.U16 else torch.uint32
+        ref = o.view(-1)[:lab.numel()].view(pdt).view(lab.shape) if pdt == torch.uint32 else \
+            o.view(torch.uint16).view(-1)[:lab.numel()].view(lab.shape)
+        mismatches += int(pn != n or lab.dtype != pdt or not torch.equal(ref.to(torch.int64), lab.to(torch.int64)))
+    peak, peak_kind = load_peaks()
+    out_bytes = sum(o.element_size() * o.numel() for o in (lab for lab, _ in got))
+    alg_bytes = voxels * 2 + out_bytes
+    gbs = alg_bytes / (ms_batch / 1e3) / 1e9
+    return {"value": voxels / ms_batch / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_batch,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_step": alg_bytes},
+            "per_volume": {"value": voxels / ms_plain / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_plain,
+                           "path": "cc3d_gpu_label_prepare + cc3d_gpu_label_finish per volume (C ABI, "
+                                   "device buffers), tile pass list/8x8 for every volume"},
+            "ratio_batched_vs_per_volume": ms_plain / ms_batch,
+            "mismatched_volumes": mismatches, "tuned": tuned,
+            "workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], one seed "
+                        "per 4096 voxels, connectivity 26, device-resident; each timed batched step in a "
+                        "fresh volume order (a new layout: its graph capture is timed)",
+            "voxels": voxels}
+
+
+def run_batch(args):
+    """The mixed-size stream as its own line: the batched and per-volume GPU
+    paths (measure_batch), the reference's CPU path on one core (a bounded
+    sample) and on every host core (the whole stream)."""
+    import cc3d_gb300 as cc3d
+    cc3d.build()
+    t0 = time.perf_counter()
+    vols = batch_stream(args.batch)
+    t_gen = time.perf_counter() - t0
+    res = measure_batch(vols, args.steps, args.warmup)
     cpu = cpu_all = None
     if not args.skip_cpu:
         import oracle
@@ -746,17 +823,10 @@ def run_batch(args):
                "kind": kind,
                "sample": f"the first {k} volumes of the stream ({done} voxels), one after another"}
         cpu_all = cpu_stream_all_cores(vols, kind)
-    print(json.dumps({
-        "metric": "GVoxels/s mixed-size stream, batched vs per-volume (bit-exact)",
-        "value": voxels / ms_batch / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_batch,
-        "per_volume_loop": {"value": voxels / ms_loop / 1e6, "ms_per_step": ms_loop},
-        "speedup_vs_per_volume": ms_loop / ms_batch,
-        "tuned": tuned, "mismatched_volumes": mismatches, "cpu_baseline": cpu,
-        "cpu_all_cores": cpu_all,
-        "config": {"workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], "
-                               "one seed per 4096 voxels, connectivity 26",
-                   "voxels": voxels, "generation_s": t_gen},
-    }), flush=True)
+    line = {"metric": "GVoxels/s mixed-size stream, batched vs per-volume (bit-exact)"}
+    line.update(res)
+    line.update({"cpu_baseline": cpu, "cpu_all_cores": cpu_all, "generation_s": t_gen})
+    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------ cost model
@@ -804,6 +874,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true", help="leave the mixed-size stream out of the line")
     ap.add_argument("--size", type=int, default=512, help="cube edge (profiling captures only)")
     ap.add_argument("--all-configs", action="store_true",
                     help="one line per benchmarked workload and tile-pass variant instead of the headline")

@@ -42,6 +42,7 @@ EXPORTED = (
     "cc3d_gpu_release_workspace",
     "cc3d_gpu_connected_components3d_noalloc",
     "cc3d_gpu_set_tile_pass",
+    "cc3d_gpu_set_union_budget",
     "cc3d_gpu_tile_pass_choice",
     "cc3d_gpu_tile_config",
     "cc3d_gpu_autotune",
@@ -117,6 +118,8 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_connected_components3d_noalloc.restype = ctypes.c_int
         lib.cc3d_gpu_set_tile_pass.argtypes = [ci]
         lib.cc3d_gpu_set_tile_pass.restype = ci
+        lib.cc3d_gpu_set_union_budget.argtypes = [ci]
+        lib.cc3d_gpu_set_union_budget.restype = ci
         lib.cc3d_gpu_tile_pass_choice.argtypes = [ci, i64, i64, i64, i64, ci]
         lib.cc3d_gpu_tile_pass_choice.restype = ci
         lib.cc3d_gpu_tile_config.argtypes = [ci]

@@ -274,6 +274,7 @@ static int label_batch(const cc3d_gpu_volume* vols, int n, int dtype, int64_t co
   if (!same_layout) {
     LabelArgs a;
     memset(&a, 0, sizeof(a));
+    a.budget = union_budget();
     a.ty = TY;
     a.tz = TZ;
     a.ntiles = tiles;

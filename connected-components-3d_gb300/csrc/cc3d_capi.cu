@@ -6,6 +6,7 @@
 // the kernel pipeline on the caller's stream and maps device error words to
 // return codes.  No C++ exception crosses the ABI.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -279,6 +280,12 @@ void cc3dgpu::record_tile_pass(int dtype, int eff_connectivity, int mode, int64_
   g_tuned[std::make_tuple(dtype, eff_connectivity, mode, size_bucket(voxels))] = variant;
 }
 
+// iteration budget of the union-find loops (0: the built-in limits)
+namespace {
+std::atomic<int> g_union_budget{0};
+}
+int cc3dgpu::union_budget() { return g_union_budget.load(std::memory_order_relaxed); }
+
 // error reporting shared with the other host translation units
 int cc3dgpu::api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int cc3dgpu::api_device_errors(unsigned err) { return check_device_errors(err); }
@@ -299,6 +306,11 @@ int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n) {
 }
 
 const char* cc3d_gpu_last_error(void) { return g_err.c_str(); }
+
+int cc3d_gpu_set_union_budget(int budget) {
+  if (budget < 0) return fail(CC3D_ERR_INVALID, "the union budget must be >= 0 (0: the built-in limits)");
+  return g_union_budget.exchange(budget);
+}
 
 const char* cc3d_gpu_version(void) { return "cc3d-gb300 0.1 (sm_103a)"; }
 
@@ -466,6 +478,7 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
 
   LabelArgs& a = job.args;
   memset(&a, 0, sizeof(a));
+  a.budget = union_budget();
   a.sx = sx; a.sy = sy; a.sz = sz;
   a.ntx = (int)((sx + kTX - 1) / kTX);
   a.nty = (int)((sy + TY - 1) / TY);

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) k_merge_edges(LabelArgs p) {
         continue;
       }
       gunite(p.E, e.x, record_node(p, otile, (int)(local >> 5), (int)(local & 31)), p.bitmap, p.nwords,
-             p.ctr);
+             p.ctr, p.budget);
     }
   }
 }
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p, int64_t ntiles) {
     for (int k = 0; k < PER; ++k) {
       const uint32_t c = base + lane + 32u * k;
       if (rc[k] != c) continue;  // not a root run: no entry of its own
-      const uint32_t R = gfind(p.E, node0 + c, p.ctr);
+      const uint32_t R = gfind(p.E, node0 + c, p.ctr, limit_of(p.budget, kFindLimit));
       const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
       const uint32_t w = key >> 5;
       uint32_t lab = 0;

@@ -91,6 +91,9 @@ inline bool device_accessible(const void* p) {
 }
 
 int api_fail(int code, const char* msg);
+// iteration budget of every union-find loop set by cc3d_gpu_set_union_budget
+// (0: the built-in limits)
+int union_budget();
 int api_device_errors(unsigned err);
 
 // per-volume results of a batch (mirrors cc3d_gpu_volume_result)

@@ -76,6 +76,9 @@ constexpr unsigned ERR_INDEX = 64u;  // an index failed its range check (access 
 constexpr int kFindLimit = 1 << 24;
 constexpr int kUniteLimit = 1 << 20;
 constexpr int kLocalLimit = 1 << 16;
+// the iteration limit of a loop: the call's budget (LabelArgs::budget, set
+// by cc3d_gpu_set_union_budget) where one is given, else the default
+__host__ __device__ __forceinline__ int limit_of(int budget, int dflt) { return budget > 0 ? budget : dflt; }
 
 struct Counters {
   unsigned int edges;        // total edges written by the tile pass
@@ -144,6 +147,7 @@ struct LabelArgs {
   // 8-connected) the image's minimum and maximum as element bits on the device
   uint64_t delta_bits;
   const unsigned long long* span;
+  int budget;                  // iteration limit of every union-find loop (0: the defaults)
 };
 
 // Geometry of the volume a tile belongs to, and the tile's place in it.
@@ -282,8 +286,9 @@ __device__ __forceinline__ int head_of(uint32_t starts, int lane) {
 }
 
 // ------------------------------------------------------ shared union-find
-__device__ __forceinline__ unsigned short sfind(volatile unsigned short* par, unsigned short n) {
-  for (int it = 0; it < kLocalLimit; ++it) {
+__device__ __forceinline__ unsigned short sfind(volatile unsigned short* par, unsigned short n,
+                                                int lim = kLocalLimit) {
+  for (int it = 0; it < lim; ++it) {
     unsigned short p = par[n];
     if (p == n) return n;
     unsigned short g = par[p];
@@ -295,8 +300,9 @@ __device__ __forceinline__ unsigned short sfind(volatile unsigned short* par, un
 
 // find without path compression: used once the unions are done, when every
 // thread only reads the forest (no write may race with the flattening)
-static __device__ __forceinline__ unsigned short sfind_ro(const volatile unsigned short* par, unsigned short n) {
-  for (int it = 0; it < kLocalLimit; ++it) {
+static __device__ __forceinline__ unsigned short sfind_ro(const volatile unsigned short* par, unsigned short n,
+                                                          int lim = kLocalLimit) {
+  for (int it = 0; it < lim; ++it) {
     const unsigned short p = par[n];
     if (p == n) return n;
     n = p;
@@ -306,11 +312,12 @@ static __device__ __forceinline__ unsigned short sfind_ro(const volatile unsigne
 
 // Inlined into its one call site in the block-parallel pass (the union
 // runner); callers with many sites use sunite_outlined.
-static __device__ __forceinline__ bool sunite(unsigned short* par, unsigned short a, unsigned short b) {
+static __device__ __forceinline__ bool sunite(unsigned short* par, unsigned short a, unsigned short b,
+                                              int lim = kLocalLimit) {
   volatile unsigned short* vp = par;
-  for (int it = 0; it < kLocalLimit; ++it) {
-    a = sfind(vp, a);
-    b = sfind(vp, b);
+  for (int it = 0; it < lim; ++it) {
+    a = sfind(vp, a, lim);
+    b = sfind(vp, b, lim);
     if (a == b) return true;
     if (a < b) { unsigned short t = a; a = b; b = t; }
     // link the larger root under the smaller one
@@ -330,8 +337,9 @@ __device__ __forceinline__ unsigned long long gload(const unsigned long long* p)
   return *(const volatile unsigned long long*)p;
 }
 
-__device__ __forceinline__ uint32_t gfind(unsigned long long* E, uint32_t n, Counters* ctr) {
-  for (int it = 0; it < kFindLimit; ++it) {
+__device__ __forceinline__ uint32_t gfind(unsigned long long* E, uint32_t n, Counters* ctr,
+                                          int lim = kFindLimit) {
+  for (int it = 0; it < lim; ++it) {
     unsigned long long e = gload(E + n);
     uint32_t p = (uint32_t)e;
     if (p == n) return n;
@@ -345,10 +353,11 @@ __device__ __forceinline__ uint32_t gfind(unsigned long long* E, uint32_t n, Cou
 }
 
 __device__ __forceinline__ void gunite(unsigned long long* E, uint32_t a, uint32_t b,
-                                       uint32_t* bitmap, int64_t nwords, Counters* ctr) {
-  for (int it = 0; it < kUniteLimit; ++it) {
-    a = gfind(E, a, ctr);
-    b = gfind(E, b, ctr);
+                                       uint32_t* bitmap, int64_t nwords, Counters* ctr, int budget = 0) {
+  const int flim = limit_of(budget, kFindLimit);
+  for (int it = 0, ulim = limit_of(budget, kUniteLimit); it < ulim; ++it) {
+    a = gfind(E, a, ctr, flim);
+    b = gfind(E, b, ctr, flim);
     if (a == b) return;
     unsigned long long ea = gload(E + a), eb = gload(E + b);
     if ((uint32_t)ea != a || (uint32_t)eb != b) continue;
@@ -444,7 +453,7 @@ __global__ void k_wrap_pairs(LabelArgs p, int conn) {
   auto at = [&](int64_t x, int64_t y, int64_t z) { return in[(z * sy + y) * sx + x]; };
   auto pair = [&](int64_t ax, int64_t ay, int64_t az, int64_t bx, int64_t by, int64_t bz) {
     if (wrap_related<T, MODE>(at(ax, ay, az), at(bx, by, bz)))
-      gunite(p.E, voxel_node(p, ax, ay, az), voxel_node(p, bx, by, bz), p.bitmap, p.nwords, p.ctr);
+      gunite(p.E, voxel_node(p, ax, ay, az), voxel_node(p, bx, by, bz), p.bitmap, p.nwords, p.ctr, p.budget);
   };
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -563,7 +572,7 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
   const uint2 ma = __ldg(p.rmask + tile * kRowsPerTile + lane), mb = __ldg(p.rmask + tile * kRowsPerTile + 32 + lane);
   const uint32_t ra = __ldg(p.rrow + tile * kRowsPerTile + lane), rb = __ldg(p.rrow + tile * kRowsPerTile + 32 + lane);
   auto root_label = [&](uint32_t c) -> uint32_t {
-    const uint32_t R = gfind(p.E, node0 + c, p.ctr);
+    const uint32_t R = gfind(p.E, node0 + c, p.ctr, limit_of(p.budget, kFindLimit));
     const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
     const uint32_t wd = key >> 5;
     if (wd >= p.nwords) {

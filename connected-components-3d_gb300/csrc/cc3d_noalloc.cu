@@ -149,6 +149,7 @@ extern "C" int cc3d_gpu_connected_components3d_noalloc(const void* in, int dtype
   const int TY = block8 ? 64 : cfg.ty, TZ = block8 ? 1 : cfg.tz, HZ = d3 ? 1 : 0;
   LabelArgs a;
   memset(&a, 0, sizeof(a));
+  a.budget = union_budget();
   a.sx = sx; a.sy = sy; a.sz = sz;
   a.ntx = (int)((sx + kTX - 1) / kTX);
   a.nty = (int)((sy + TY - 1) / TY);

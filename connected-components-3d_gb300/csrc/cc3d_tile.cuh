@@ -74,7 +74,7 @@ struct BoxRow {
 // queue site shares one copy of the union-find code.  Returns 2 for a node id
 // out of range, 1 if a union ran out of budget, else 0.
 static __device__ __noinline__ int run_unions(const uint32_t* q, int from, int to, unsigned short* par, int nodes,
-                                       int lane) {
+                                       int lane, int lim) {
   __syncwarp();
   int err = 0;
   for (int r = from; r < to; r += 32) {
@@ -83,7 +83,7 @@ static __device__ __noinline__ int run_unions(const uint32_t* q, int from, int t
       const uint32_t e = q[i];
       const int a = (int)(e >> 16), b = (int)(e & 0xFFFFu);
       if (a >= nodes || b >= nodes) err = 2;
-      else if (!sunite(par, (unsigned short)a, (unsigned short)b)) err = 1;
+      else if (!sunite(par, (unsigned short)a, (unsigned short)b, lim)) err = 1;
     }
   }
   __syncwarp();
@@ -149,6 +149,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const int tx = g.tx;
   const int64_t x0 = (int64_t)tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   const uint32_t lt = (1u << lane) - 1u;
+  const int llim = limit_of(p.budget, kLocalLimit);
 
   auto is_tile_row = [&](int rb) -> bool {
     const int by = rb % BY, bz = rb / BY;
@@ -335,7 +336,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // run whole rounds of 32 from the top of the queue
   auto flush = [&](int keep) {
     if (uqn > keep) {
-      const int e = run_unions(myq, keep, uqn, par, NODES, lane);
+      const int e = run_unions(myq, keep, uqn, par, NODES, lane, llim);
       if (e) local_err = e;
       uqn = keep;
     }
@@ -454,7 +455,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     bool root = false;
     if ((Sr >> lane) & 1u) {
       const unsigned short n = (unsigned short)(ri * 32 + lane);
-      const unsigned short r = sfind_ro(par, n);
+      const unsigned short r = sfind_ro(par, n, llim);
       par[n] = r;
       root = (r == n);
     }
@@ -558,7 +559,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       node = (unsigned short)(CNODE + c);
       if (GRAPH ? !((vcol[GRAPH ? rb : 0] >> (c < NRB ? 0 : 1)) & 1u) : !is_fg(sv(rb, xi))) return false;
     }
-    const unsigned short r = sfind_ro(par, node);
+    const unsigned short r = sfind_ro(par, node, llim);
     if (r >= kTV) return false;
     const int rp = MODE == MODE_BINARY4 ? -1 : prev_row(rb);
     if (rp >= 0) {
@@ -578,7 +579,7 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
         if (xi < 0) np = (unsigned short)(CNODE + rp);
         else if (xi > 31) np = (unsigned short)(CNODE + NRB + rp);
         else np = (unsigned short)(HNODE + rp * 32 + head_of(smask[rp], xi));
-        if (sfind_ro(par, np) == r) return false;
+        if (sfind_ro(par, np, llim) == r) return false;
       }
     }
     const int by = rb % BY, bz = rb / BY;

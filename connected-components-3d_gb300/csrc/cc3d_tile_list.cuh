@@ -100,8 +100,8 @@ template <> struct NeedRels<4> {
 // smaller root, so the root of every tree is its smallest node.  Every loop
 // is bounded.
 template <typename PT>
-static __device__ __forceinline__ uint32_t lfind(volatile PT* par, uint32_t n) {
-  for (int it = 0; it < kLocalLimit; ++it) {
+static __device__ __forceinline__ uint32_t lfind(volatile PT* par, uint32_t n, int lim) {
+  for (int it = 0; it < lim; ++it) {
     const uint32_t p = par[n];
     if (p == n) return n;
     const uint32_t g = par[p];
@@ -111,8 +111,8 @@ static __device__ __forceinline__ uint32_t lfind(volatile PT* par, uint32_t n) {
   return n;
 }
 template <typename PT>
-static __device__ __forceinline__ uint32_t lfind_ro(const volatile PT* par, uint32_t n) {
-  for (int it = 0; it < kLocalLimit; ++it) {
+static __device__ __forceinline__ uint32_t lfind_ro(const volatile PT* par, uint32_t n, int lim) {
+  for (int it = 0; it < lim; ++it) {
     const uint32_t p = par[n];
     if (p == n) return n;
     n = p;
@@ -120,11 +120,11 @@ static __device__ __forceinline__ uint32_t lfind_ro(const volatile PT* par, uint
   return n;
 }
 template <typename PT>
-static __device__ __forceinline__ bool lunite(PT* par, uint32_t a, uint32_t b) {
+static __device__ __forceinline__ bool lunite(PT* par, uint32_t a, uint32_t b, int lim) {
   volatile PT* vp = par;
-  for (int it = 0; it < kLocalLimit; ++it) {
-    a = lfind<PT>(vp, a);
-    b = lfind<PT>(vp, b);
+  for (int it = 0; it < lim; ++it) {
+    a = lfind<PT>(vp, a, lim);
+    b = lfind<PT>(vp, b, lim);
     if (a == b) return true;
     if (a < b) { const uint32_t t = a; a = b; b = t; }
     if ((uint32_t)atomicCAS(par + a, (PT)a, (PT)b) == a) return true;
@@ -196,6 +196,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const uint32_t node0 = utile * (uint32_t)kTV;
   const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   const uint32_t lt = (1u << lane) - 1u;
+  const int llim = limit_of(p.budget, kLocalLimit);
 
   auto box_row_of = [&](int ri) -> int { return (ri / TY + HZ) * BY + (ri % TY) + 1; };
   auto at = [&](int rb, int x) -> T { return box[rb * W + PADX + x]; };
@@ -382,7 +383,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     for (int r0 = 0; r0 < pc; r0 += 32) {
       if (r0 + lane < pc) {
         const uint32_t q = pw[r0 + lane];
-        if (!lunite<PT>(par, q >> 16, q & 0xFFFFu)) err = 1;
+        if (!lunite<PT>(par, q >> 16, q & 0xFFFFu, llim)) err = 1;
       }
     }
     __syncwarp();
@@ -471,7 +472,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     uint32_t r = 0;
     if ((S >> lane) & 1u) {
       const uint32_t n = nbase[rb] + lane;
-      r = lfind_ro<PT>(par, n);
+      r = lfind_ro<PT>(par, n, llim);
       par[n] = (PT)r;
       root = r == n;
     }
@@ -493,7 +494,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   }
   for (int c = tid; c < 2 * NRB; c += kThreads) {
     const uint32_t n = (uint32_t)(CNODE + c);
-    par[n] = (PT)lfind_ro<PT>(par, n);
+    par[n] = (PT)lfind_ro<PT>(par, n, llim);
   }
   __syncthreads();
 

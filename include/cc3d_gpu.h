@@ -223,6 +223,19 @@ int cc3d_gpu_statistics(
 void cc3d_gpu_profile_enable(int enable);
 int cc3d_gpu_profile_read(double* ms, uint64_t* launches, int n);
 
+/*
+ * Iteration budget of every bounded union-find loop on the device (the find,
+ * union and tile-union loops of the labelling kernels), for all threads of
+ * the process; 0 (the default) restores the built-in limits.  A labelling
+ * whose loops run out of budget stops them, skips the rest of their work and
+ * returns CC3D_ERR_DEVICE ("... union budget ..." / "find budget"); the GPU
+ * stays usable and the next call with an adequate budget is exact.  For
+ * testing the give-up path: the reference has no counterpart (its
+ * DisjointSet throws when its label array is full, cc3d/cc3d.hpp:107-111).
+ * Returns the previous budget, or CC3D_ERR_INVALID for a negative one.
+ */
+int cc3d_gpu_set_union_budget(int budget);
+
 /* Release this thread's cached device workspace. */
 void cc3d_gpu_release_workspace(void);
 
