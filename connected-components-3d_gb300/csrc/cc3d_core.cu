@@ -35,8 +35,8 @@ __global__ void __launch_bounds__(256) k_merge_edges(LabelArgs p) {
         atomicOr(&p.ctr->err, ERR_INDEX);
         continue;
       }
-      gunite(p.E, e.x, record_node(p, otile, (int)(local >> 5), (int)(local & 31)), p.bitmap, p.nwords,
-             p.ctr, p.budget);
+      gunite(p.E, e.x, record_node(p, otile, (int)(local >> 5), (int)(local & 31)), node_count(p), p.bitmap,
+             p.nwords, p.ctr, p.budget);
     }
   }
 }
@@ -202,7 +202,11 @@ __global__ void __launch_bounds__(256) k_resolve(LabelArgs p, int64_t ntiles) {
     for (int k = 0; k < PER; ++k) {
       const uint32_t c = base + lane + 32u * k;
       if (rc[k] != c) continue;  // not a root run: no entry of its own
-      const uint32_t R = gfind(p.E, node0 + c, p.ctr, limit_of(p.budget, kFindLimit));
+      const uint32_t R = gfind(p.E, node0 + c, node_count(p), p.ctr, limit_of(p.budget, kFindLimit));
+      if (R == kBadNode) {
+        p.label[node0 + c] = 0u;
+        continue;
+      }
       const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
       const uint32_t w = key >> 5;
       uint32_t lab = 0;

@@ -337,27 +337,43 @@ __device__ __forceinline__ unsigned long long gload(const unsigned long long* p)
   return *(const volatile unsigned long long*)p;
 }
 
-__device__ __forceinline__ uint32_t gfind(unsigned long long* E, uint32_t n, Counters* ctr,
+// Root of node n among the nn nodes of E.  Every parent is range-checked: a
+// parent outside [0, nn) sets ERR_INDEX and returns kBadNode, so a corrupt
+// entry raises the error word instead of reading outside E.  When the budget
+// runs out the node reached so far is returned (with ERR_FIND_BUDGET set).
+constexpr uint32_t kBadNode = 0xFFFFFFFFu;
+__device__ __forceinline__ uint32_t gfind(unsigned long long* E, uint32_t n, uint32_t nn, Counters* ctr,
                                           int lim = kFindLimit) {
+  if (n >= nn) {
+    atomicOr(&ctr->err, ERR_INDEX);
+    return kBadNode;
+  }
   for (int it = 0; it < lim; ++it) {
     unsigned long long e = gload(E + n);
     uint32_t p = (uint32_t)e;
     if (p == n) return n;
+    if (p >= nn) break;
     unsigned long long e2 = gload(E + p);
     uint32_t g = (uint32_t)e2;
+    if (g >= nn) break;
     if (g != p) *(volatile unsigned long long*)(E + n) = e2;  // path halving
     n = g;
+    if (it + 1 == lim) {
+      atomicOr(&ctr->err, ERR_FIND_BUDGET);
+      return n;
+    }
   }
-  atomicOr(&ctr->err, ERR_FIND_BUDGET);
-  return n;
+  atomicOr(&ctr->err, ERR_INDEX);
+  return kBadNode;
 }
 
-__device__ __forceinline__ void gunite(unsigned long long* E, uint32_t a, uint32_t b,
+__device__ __forceinline__ void gunite(unsigned long long* E, uint32_t a, uint32_t b, uint32_t nn,
                                        uint32_t* bitmap, int64_t nwords, Counters* ctr, int budget = 0) {
   const int flim = limit_of(budget, kFindLimit);
   for (int it = 0, ulim = limit_of(budget, kUniteLimit); it < ulim; ++it) {
-    a = gfind(E, a, ctr, flim);
-    b = gfind(E, b, ctr, flim);
+    a = gfind(E, a, nn, ctr, flim);
+    b = gfind(E, b, nn, ctr, flim);
+    if (a == kBadNode || b == kBadNode) return;
     if (a == b) return;
     unsigned long long ea = gload(E + a), eb = gload(E + b);
     if ((uint32_t)ea != a || (uint32_t)eb != b) continue;
@@ -375,6 +391,12 @@ __device__ __forceinline__ void gunite(unsigned long long* E, uint32_t a, uint32
     }
   }
   atomicOr(&ctr->err, ERR_UNITE_BUDGET);
+}
+
+// number of component nodes of a labelling (node ids fit 32 bits)
+__device__ __forceinline__ uint32_t node_count(const LabelArgs& p) {
+  const uint64_t n = (uint64_t)p.ntiles * kTV;
+  return n < 0xFFFFFFFFull ? (uint32_t)n : 0xFFFFFFFFu;
 }
 
 // component node of a voxel given its tile and in-tile position (x & 31, row);
@@ -453,7 +475,8 @@ __global__ void k_wrap_pairs(LabelArgs p, int conn) {
   auto at = [&](int64_t x, int64_t y, int64_t z) { return in[(z * sy + y) * sx + x]; };
   auto pair = [&](int64_t ax, int64_t ay, int64_t az, int64_t bx, int64_t by, int64_t bz) {
     if (wrap_related<T, MODE>(at(ax, ay, az), at(bx, by, bz)))
-      gunite(p.E, voxel_node(p, ax, ay, az), voxel_node(p, bx, by, bz), p.bitmap, p.nwords, p.ctr, p.budget);
+      gunite(p.E, voxel_node(p, ax, ay, az), voxel_node(p, bx, by, bz), node_count(p), p.bitmap, p.nwords, p.ctr,
+             p.budget);
   };
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -572,7 +595,8 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
   const uint2 ma = __ldg(p.rmask + tile * kRowsPerTile + lane), mb = __ldg(p.rmask + tile * kRowsPerTile + 32 + lane);
   const uint32_t ra = __ldg(p.rrow + tile * kRowsPerTile + lane), rb = __ldg(p.rrow + tile * kRowsPerTile + 32 + lane);
   auto root_label = [&](uint32_t c) -> uint32_t {
-    const uint32_t R = gfind(p.E, node0 + c, p.ctr, limit_of(p.budget, kFindLimit));
+    const uint32_t R = gfind(p.E, node0 + c, node_count(p), p.ctr, limit_of(p.budget, kFindLimit));
+    if (R == kBadNode) return 0u;
     const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
     const uint32_t wd = key >> 5;
     if (wd >= p.nwords) {

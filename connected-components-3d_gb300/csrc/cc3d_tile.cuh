@@ -455,7 +455,13 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     bool root = false;
     if ((Sr >> lane) & 1u) {
       const unsigned short n = (unsigned short)(ri * 32 + lane);
-      const unsigned short r = sfind_ro(par, n, llim);
+      unsigned short r = sfind_ro(par, n, llim);
+      if (par[r] != r) {
+        // the find ran out of budget: the run becomes a root of its own (the
+        // call reports the error), so every component id stays defined
+        local_err = 1;
+        r = n;
+      }
       par[n] = r;
       root = (r == n);
     }
@@ -559,8 +565,11 @@ k_tile_runs(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       node = (unsigned short)(CNODE + c);
       if (GRAPH ? !((vcol[GRAPH ? rb : 0] >> (c < NRB ? 0 : 1)) & 1u) : !is_fg(sv(rb, xi))) return false;
     }
-    const unsigned short r = sfind_ro(par, node, llim);
+    unsigned short r = sfind_ro(par, node, llim);
     if (r >= kTV) return false;
+    // a find that ran out of budget ends on a tile run head, whose parent is
+    // its root after phase 3a (the error is already recorded)
+    if (par[r] != r) r = par[r];
     const int rp = MODE == MODE_BINARY4 ? -1 : prev_row(rb);
     if (rp >= 0) {
       const S a = sv(rb, xi), b = sv(rp, xi);

@@ -473,6 +473,12 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     if ((S >> lane) & 1u) {
       const uint32_t n = nbase[rb] + lane;
       r = lfind_ro<PT>(par, n, llim);
+      if (par[r] != r) {
+        // the find ran out of budget: the run becomes a root of its own (the
+        // call reports the error), so every component it names has a key
+        local_err = 1;
+        r = n;
+      }
       par[n] = (PT)r;
       root = r == n;
     }
@@ -494,7 +500,12 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   }
   for (int c = tid; c < 2 * NRB; c += kThreads) {
     const uint32_t n = (uint32_t)(CNODE + c);
-    par[n] = (PT)lfind_ro<PT>(par, n, llim);
+    uint32_t r = lfind_ro<PT>(par, n, llim);
+    if (par[r] != r) {
+      local_err = 1;
+      r = n;
+    }
+    par[n] = (PT)r;
   }
   __syncthreads();
 
