@@ -62,6 +62,11 @@ EXPORTED = (
     "cc3d_gpu_contacts_copy",
     "cc3d_gpu_run_starts",
     "cc3d_gpu_run_starts_copy",
+    "cc3d_gpu_stack_work_bytes",
+    "cc3d_gpu_stack_begin",
+    "cc3d_gpu_stack_seam",
+    "cc3d_gpu_stack_number",
+    "cc3d_gpu_stack_relabel",
 )
 PROFILE_STAGES = ("h2d", "epl", "tile_local", "merge_edges", "wrap_pairs", "scan", "write", "d2h")
 
@@ -156,6 +161,17 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_run_starts_copy.argtypes = [vp, vp, ctypes.c_uint64]
         lib.cc3d_gpu_run_starts_copy.restype = ci
         lib.cc3d_gpu_zero_labels.restype = ci
+        u64 = ctypes.c_uint64
+        lib.cc3d_gpu_stack_work_bytes.argtypes = [u64]
+        lib.cc3d_gpu_stack_work_bytes.restype = u64
+        lib.cc3d_gpu_stack_begin.argtypes = [vp, u64, vp]
+        lib.cc3d_gpu_stack_seam.argtypes = [vp, vp, ci, vp, ci, u64, vp, ci, u64, i64, i64, i64, ci, vp, u64, vp]
+        lib.cc3d_gpu_stack_number.argtypes = [vp, u64, u64p, vp]
+        lib.cc3d_gpu_stack_relabel.argtypes = [vp, ci, i64p, u64, vp, ci, i64p, i64, i64, i64, vp, u64,
+                                               ctypes.POINTER(ci), vp]
+        for name in ("cc3d_gpu_stack_begin", "cc3d_gpu_stack_seam", "cc3d_gpu_stack_number",
+                     "cc3d_gpu_stack_relabel"):
+            getattr(lib, name).restype = ci
         for name in ("cc3d_gpu_volume_features", "cc3d_gpu_cost_model_train", "cc3d_gpu_cost_model_predict",
                      "cc3d_gpu_cost_model_get", "cc3d_gpu_cost_model_set", "cc3d_gpu_cost_model_choose"):
             getattr(lib, name).restype = ci

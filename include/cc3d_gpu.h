@@ -289,6 +289,49 @@ int cc3d_gpu_run_starts(const void* labels, int label_bytes, int64_t voxels, uin
 int cc3d_gpu_run_starts_copy(uint64_t* positions, uint64_t* labels, uint64_t nstarts);
 
 /*
+ * The seam merge of cc3d.connected_components_stack on the device
+ * (cc3d/__init__.py:324-501; the reference's DisjointSet at :296-321, its
+ * seam loops at :425-463 and the final crackle.renumber at :488-495).  The
+ * caller labels every slab on its own (local labels 1..n_k) and gives slab k
+ * the global labels offset_k + 1 .. offset_k + n_k, offset_k = n_0 + ... +
+ * n_{k-1}; total_labels = the sum of all n_k.  A device work area of
+ * cc3d_gpu_stack_work_bytes(total_labels) bytes holds a union-find table
+ * over the global labels.
+ *   cc3d_gpu_stack_begin: every label is its own group.
+ *   cc3d_gpu_stack_seam: joins the groups of every pair of labels that touch
+ *     across one seam: the bottom plane (the last plane of slab k-1) against
+ *     the top plane (the first plane of slab k).  Planes are sx * sy device
+ *     arrays indexed x * sy + y (the reference's image[x, y, z] with z
+ *     fixed); the images' dtype code (CC3D_U8..CC3D_F64, or CC3D_F16)
+ *     decides equality (value equality for floats, as numpy's ==) unless
+ *     binary_image, where both must be nonzero.  Connectivity 6: the voxel
+ *     straight across; 26: the 3 x 3 patch across.
+ *   cc3d_gpu_stack_number: each group's number is the rank of its smallest
+ *     label among all groups' smallest labels (1..N); N is returned.
+ *   cc3d_gpu_stack_relabel: out[x, y, z] = number of (offset + labels[x, y,
+ *     z]) (0 for label 0) for a slab of sx * sy * sz voxels read and written
+ *     with element strides (x, y, z), so a slab lands in place in the whole
+ *     volume's output; *has_background (if not null) is set when any voxel
+ *     of the slab is 0.
+ * Labels outside the table give CC3D_ERR_INVALID; a union-find loop that runs
+ * out of its iteration budget gives CC3D_ERR_DEVICE.  number and relabel
+ * synchronise `stream`.
+ */
+#define CC3D_F16 7 /* float16 images: accepted by cc3d_gpu_stack_seam */
+uint64_t cc3d_gpu_stack_work_bytes(uint64_t total_labels);
+int cc3d_gpu_stack_begin(void* work, uint64_t total_labels, void* stream);
+int cc3d_gpu_stack_seam(const void* bottom_img, const void* top_img, int img_dtype,
+                        const void* bottom_labels, int bottom_label_bytes, uint64_t bottom_offset,
+                        const void* top_labels, int top_label_bytes, uint64_t top_offset, int64_t sx,
+                        int64_t sy, int64_t connectivity, int binary_image, void* work,
+                        uint64_t total_labels, void* stream);
+int cc3d_gpu_stack_number(void* work, uint64_t total_labels, uint64_t* N, void* stream);
+int cc3d_gpu_stack_relabel(const void* labels, int label_bytes, const int64_t* label_strides,
+                           uint64_t offset, void* out, int out_bytes, const int64_t* out_strides,
+                           int64_t sx, int64_t sy, int64_t sz, void* work, uint64_t total_labels,
+                           int* has_background, void* stream);
+
+/*
  * Tile-pass configurations and their autotuner.  No counterpart in the
  * reference, which has a single CPU algorithm per connectivity.  Every
  * configuration gives identical labels; they differ only in speed.

@@ -537,3 +537,85 @@ def color_connectivity_graph(vcg: np.ndarray, connectivity: int = 26, return_N: 
     while out.ndim > dims:
         out = out[..., 0]
     return (out, int(ncomp)) if return_N else out
+
+
+def _stack_seam_pairs(bottom_img, bottom_lab, top_img, top_lab, connectivity: int, binary_image: bool):
+    """(bottom label, top label) pairs joined across one seam: the reference's
+    seam loops (cc3d/__init__.py:425-463) as array operations.  For 26 the
+    reference skips a voxel's diagonals once the voxel straight above joins;
+    those diagonals join top voxels already joined to that one, so every
+    offset can be taken."""
+    sx, sy = bottom_img.shape
+    offs = [(0, 0)] if connectivity == 6 else [(dx, dy) for dx in (-1, 0, 1) for dy in (-1, 0, 1)]
+    pairs = []
+    for dx, dy in offs:
+        bx = slice(max(0, -dx), sx - max(0, dx))
+        by = slice(max(0, -dy), sy - max(0, dy))
+        tx = slice(max(0, dx), sx + min(0, dx))
+        ty = slice(max(0, dy), sy + min(0, dy))
+        bl, tl = bottom_lab[bx, by], top_lab[tx, ty]
+        bi, ti = bottom_img[bx, by], top_img[tx, ty]
+        rel = (bi != 0) & (ti != 0) if binary_image else (bi == ti)
+        m = (bl != 0) & (tl != 0) & rel
+        if m.any():
+            pairs.append(np.stack([bl[m], tl[m]], axis=1))
+    return np.concatenate(pairs) if pairs else np.zeros((0, 2), np.uint64)
+
+
+def connected_components_stack(stacked_images, connectivity: int = 26, return_N: bool = False,
+                               binary_image: bool = False):
+    """Restatement of cc3d.connected_components_stack (cc3d/__init__.py:324-501)
+    on the CPU: every slab labelled by this oracle with uint64 labels offset by
+    the slabs before it, seam pairs joined in a disjoint set whose root is the
+    smallest label (cc3d/__init__.py:296-321), and the groups numbered 1..N in
+    increasing order of their smallest label (crackle.renumber of the sorted
+    labels).  Returns (labels in Fortran order, N, has_background) -- the
+    crackle array itself is not restated."""
+    if connectivity not in (6, 26):
+        raise ValueError(f"Connectivity must be 6 or 26. Got: {connectivity}")
+    slabs, pairs = [], []
+    offset = 0
+    prev_img = prev_lab = None
+    for image in stacked_images:
+        image = np.asarray(image)
+        cc, n = connected_components(image, connectivity=connectivity, return_N=True, out_dtype=np.uint64,
+                                     binary_image=bool(binary_image))
+        cc = np.asarray(cc)
+        if offset:
+            np.add(cc, np.uint64(offset), out=cc, where=(cc != 0))
+        if prev_img is not None:
+            pairs.append(_stack_seam_pairs(prev_img, prev_lab, image[:, :, 0], cc[:, :, 0], connectivity,
+                                           bool(binary_image)))
+        offset += int(n)
+        slabs.append(cc)
+        prev_img, prev_lab = image[:, :, -1], cc[:, :, -1]
+    if not slabs:
+        raise ValueError("no images to stack")
+    rep = np.arange(offset + 1, dtype=np.uint64)
+    allp = np.concatenate(pairs) if pairs else np.zeros((0, 2), np.uint64)
+    if len(allp):
+        import scipy.sparse as sp
+        from scipy.sparse.csgraph import connected_components as graph_components
+        nodes, inv = np.unique(allp.reshape(-1), return_inverse=True)
+        inv = inv.reshape(-1, 2)
+        g = sp.coo_matrix((np.ones(len(inv), np.int8), (inv[:, 0], inv[:, 1])), shape=(len(nodes), len(nodes)))
+        ncomp, comp = graph_components(g, directed=False)
+        smallest = np.full(ncomp, np.iinfo(np.uint64).max, dtype=np.uint64)
+        np.minimum.at(smallest, comp, nodes)
+        rep[nodes.astype(np.int64)] = smallest[comp]
+    uniq = np.unique(rep[1:])
+    N = int(len(uniq))
+    table = np.zeros(offset + 1, dtype=np.uint64)
+    table[1:] = np.searchsorted(uniq, rep[1:]) + 1
+    out_dtype = next(np.dtype(t) for t in (np.uint8, np.uint16, np.uint32, np.uint64) if N <= np.iinfo(t).max)
+    table = table.astype(out_dtype)
+    depth = sum(s.shape[2] for s in slabs)
+    out = np.empty(slabs[0].shape[:2] + (depth,), dtype=out_dtype, order="F")
+    z = 0
+    has_bg = False
+    for cc in slabs:
+        d = cc.shape[2]
+        out[:, :, z:z + d] = table[cc.astype(np.int64)]
+        has_bg = has_bg or bool((cc == 0).any())
+        z += d
+    return (out, N, has_bg) if return_N else out
