@@ -746,6 +746,13 @@ def measure_batch(vols, steps: int, warmup: int) -> dict:
         return max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3) / k
 
     ms_batch = timed(batched, steps)
+    # the same stream through the staged batcher (one launch per stage, its
+    # graph captured per layout: every step is a new layout)
+    prev_mode = cc3d.set_batch_mode("staged")
+    try:
+        ms_staged = timed(batched, steps)
+    finally:
+        cc3d.set_batch_mode(prev_mode)
     # the plain path: per-volume C ABI calls, preallocated uint32 outputs
     outs = [torch.empty(d.shape, dtype=torch.uint32, device="cuda") for d in dev]
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -789,6 +796,9 @@ def measure_batch(vols, steps: int, warmup: int) -> dict:
                            "path": "cc3d_gpu_label_prepare + cc3d_gpu_label_finish per volume (C ABI, "
                                    "device buffers), tile pass list/8x8 for every volume"},
             "ratio_batched_vs_per_volume": ms_plain / ms_batch,
+            "staged": {"value": voxels / ms_staged / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_staged,
+                       "path": "one launch per stage, the stage graph captured per layout (tuned tile pass)"},
+            "mode": "persistent: one cooperative kernel launch per batch, replayed from a CUDA graph",
             "mismatched_volumes": mismatches, "tuned": tuned,
             "workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], one seed "
                         "per 4096 voxels, connectivity 26, device-resident; each timed batched step in a "

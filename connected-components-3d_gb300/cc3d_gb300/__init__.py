@@ -13,7 +13,7 @@ from .api import (  # noqa: F401
 )
 from . import _native  # noqa: F401
 from .tuning import autotune, autotune_reset, set_tile_pass, tile_pass_choice  # noqa: F401
-from .batch import autotune_batch, connected_components_batch  # noqa: F401
+from .batch import autotune_batch, connected_components_batch, set_batch_mode  # noqa: F401
 from . import costmodel, tuning  # noqa: F401
 from .filters import dust, largest_k  # noqa: F401
 from .stack import LabelStack, connected_components_stack  # noqa: F401
@@ -27,6 +27,7 @@ __all__ = [
     "statistics",
     "DimensionError",
     "connected_components_batch",
+    "set_batch_mode",
     "dust",
     "largest_k",
     "contacts",

@@ -50,6 +50,7 @@ EXPORTED = (
     "cc3d_gpu_label_batch",
     "cc3d_gpu_release_batch",
     "cc3d_gpu_autotune_batch",
+    "cc3d_gpu_set_batch_mode",
     "cc3d_gpu_volume_features",
     "cc3d_gpu_cost_model_train",
     "cc3d_gpu_cost_model_predict",
@@ -141,6 +142,8 @@ def load() -> ctypes.CDLL:
         lib.cc3d_gpu_autotune_batch.argtypes = [vp, ci, ci, i64, vp, vp, ci, ctypes.POINTER(ci),
                                                 ctypes.POINTER(ctypes.c_double)]
         lib.cc3d_gpu_autotune_batch.restype = ci
+        lib.cc3d_gpu_set_batch_mode.argtypes = [ci]
+        lib.cc3d_gpu_set_batch_mode.restype = ci
         fp = ctypes.POINTER(ctypes.c_float)
         lib.cc3d_gpu_volume_features.argtypes = [vp, ci, i64, i64, i64, i64, ci, ci, vp, fp]
         lib.cc3d_gpu_cost_model_train.argtypes = [vp, vp, ci, ci, ci, ctypes.c_float, ctypes.c_uint64, fp]

@@ -4,9 +4,12 @@
 
 gives, for every volume, exactly what ``connected_components(vol,
 connectivity)`` gives (labels, N, and the output dtype the reference would
-choose), but labels all of them with one launch of each stage, replayed from a
-CUDA graph while the list of shapes repeats.  The reference has no batch call:
-its users loop over ``cc3d.connected_components``.
+choose), but labels all of them together: by default with ONE persistent
+kernel launch that walks every stage over the whole batch (replayed from a
+CUDA graph captured once, whatever the shapes), or, after
+``set_batch_mode("staged")``, with one launch of each stage replayed from a
+CUDA graph while the list of shapes repeats.  The reference has no batch
+call: its users loop over ``cc3d.connected_components``.
 
 Volumes are CUDA tensors or numpy arrays (copied to the device) of one dtype
 among uint8/16/32 (int8/16/32 and bool are viewed as the unsigned type of the
@@ -97,6 +100,19 @@ def _labels(devs, outs, res, return_N):
             lab = outs[i][:nbytes].view(tdt).view(d.shape)
         results.append((lab, int(Ns[i])) if return_N else lab)
     return results
+
+
+_MODES = {"persistent": 0, "staged": 1}
+
+
+def set_batch_mode(mode: str) -> str:
+    """This thread's batch mode, "persistent" (default) or "staged"; returns
+    the previous one (cc3d_gpu_set_batch_mode)."""
+    if mode not in _MODES:
+        raise ValueError(f"unknown batch mode {mode!r}")
+    prev = nat.load().cc3d_gpu_set_batch_mode(_MODES[mode])
+    nat.check(min(prev, 0))
+    return {v: k for k, v in _MODES.items()}[prev]
 
 
 def connected_components_batch(volumes: Sequence[Any], connectivity: int = 26,

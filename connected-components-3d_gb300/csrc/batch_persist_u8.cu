@@ -1,0 +1,5 @@
+// the persistent batch kernels of uint8_t volumes (cc3d_batch_persistent.cuh)
+#include "cc3d_batch_persistent.cuh"
+namespace cc3dgpu {
+const void* persistent_kernel_u8(int conn) { return persistent_kernel<uint8_t>(conn); }
+}  // namespace cc3dgpu

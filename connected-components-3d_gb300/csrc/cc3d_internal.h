@@ -119,6 +119,10 @@ cudaError_t launch_write_tiles(const LabelArgs& a, void* out, int out_dtype, int
 cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, BatchResult* res,
                                   cudaStream_t s);
 cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s);
+// the persistent batch kernels k_batch_persistent<T, conn> (batch_persist_*.cu)
+const void* persistent_kernel_u8(int conn);
+const void* persistent_kernel_u16(int conn);
+const void* persistent_kernel_u32(int conn);
 
 // statistics (cc3d_stats.cu)
 struct StatsArgs {

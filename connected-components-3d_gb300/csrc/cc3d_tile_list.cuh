@@ -132,9 +132,26 @@ static __device__ __forceinline__ bool lunite(PT* par, uint32_t a, uint32_t b, i
   return false;
 }
 
+// Tile rows of warp w: the j-th of its 8 rows.  A warp owns whole columns of
+// rows along the link direction (z in 3D, y in 2D) and takes them from the
+// bottom up, so the link row of its j-th row is, for all but its first rows,
+// one of its own earlier rows: by the time a warp resolves a row's roots, the
+// link row's runs already point at theirs and the finds stay short.
+template <int TY>
+__device__ __forceinline__ int warp_row(int w, int j) {
+  if constexpr (TY == 16) return (w + 8 * (j & 1)) + 16 * (j >> 1);
+  else if constexpr (TY == 8) return w + 8 * j;
+  else if constexpr (TY == 4) return (w & 3) + 4 * (8 * (w >> 2) + j);
+  else return 8 * w + j;  // 2D: 64 x 1 tiles
+}
+
+// One tile of the list pass, by the whole 256-thread block: the kernel below
+// runs one per block; the persistent batch kernel (cc3d_batch_persistent.cu)
+// runs many in a row (the block's shared memory is free again once it
+// returns).  `tmap` is used only when use_tma is set.
 template <typename T, int CONN, int TY, int TZ, int MODE>
-__global__ void __launch_bounds__(kThreads, 6)
-k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
+__device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtensorMap* tmap, int use_tma,
+                                               int64_t tile) {
   static_assert(MODE == MODE_MULTI || MODE == MODE_BINARY, "multilabel or binary relation");
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
   constexpr int HZ = D3 ? 1 : 0;
@@ -146,6 +163,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int CNODE = kTV + NHR * 32;  // columns: CNODE + rb (x0 - 1), CNODE + NRB + rb (x0 + 32)
   constexpr int NODES = CNODE + 2 * NRB;
   constexpr int NW = kThreads / 32;
+  constexpr int RPW = NR / NW;           // tile rows per warp
   constexpr int NRN = RowNb<CONN>::n;
   constexpr int W = BoxRow<T>::W, PADX = BoxRow<T>::PADX;
   // a primary neighbour row decides most voxels (26, 18: below; 8: behind)
@@ -153,29 +171,28 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   // the link row: every run's first pair of runs with it becomes a direct
   // parent link (below in 3D, behind in 2D)
   constexpr int LOFF = D3 ? -BY : -1;
+  constexpr int LSTEP = D3 ? TY : 1;     // tile-row distance to the link row
   constexpr int LROW0 = D3 ? TY : 1;     // first tile row whose link row is a tile row
-  constexpr int QN = (NR / NW) * 32;     // list capacity: every voxel of the warp's rows
+  constexpr int QN = RPW * 32;           // list capacity: every voxel of the warp's rows
   using NRel = NeedRels<CONN>;
   constexpr int NB = NRel::n;
   static_assert(kTX * NR == kTV, "tile must hold 2048 voxels");
   static_assert(NR == kRowsPerTile, "64 rows per tile");
-  static_assert(NR % NW == 0, "rows per warp");
+  static_assert(RPW == 8, "8 rows per warp");
   static_assert(NODES < 16384, "node ids must fit 14 bits");
   static_assert(W <= 256 && BY <= 256 && BZ <= 256, "TMA box dimensions");
-  static_assert(NRB < 255, "box rows fit a byte");
 
   __shared__ __align__(128) T box[NRB * W];
   __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t smask[NRB], fmask[NRB];
   using PT = typename std::conditional<sizeof(T) == 8, unsigned short, uint32_t>::type;
   __shared__ __align__(16) PT par[NODES];
-  // per box row: node id of its voxel 0; the tile holding its 32 voxels and
-  // the row's index inside that tile; the same-owner box row before it (one
-  // back in y, else in z; 255: none); global row index y + sy * z; flags
-  // (bit 0: tile row, bit 1: inside the volume)
-  __shared__ unsigned short nbase[NRB], rloc[NRB];
-  __shared__ uint32_t rtile[NRB], rgrow[NRB];
-  __shared__ unsigned char rprev[NRB], rflag[NRB];
+  __shared__ unsigned short nbase[NRB];     // node id of every box row's voxel 0
+  // per box row: the tile holding its 32 voxels and the row's index inside
+  // that tile; the same-owner box row before it (one back in y, else in z;
+  // 255: none)
+  __shared__ uint32_t rtile[NRB];
+  __shared__ unsigned char rloc[NRB], rprev[NRB];
   // per warp: one entry per voxel of its rows that has unions to run:
   // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x
   __shared__ unsigned short ulist[NW][QN];
@@ -183,6 +200,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   constexpr int PC = 64;
   __shared__ uint32_t pairs[NW][PC];
   __shared__ unsigned short rbase[NR + 1];  // first run of every tile row
+  __shared__ uint32_t rootm[NR];            // root runs of every tile row
   __shared__ unsigned long long red_epl[NW];
   __shared__ int red_first[NW], red_last[NW];
   __shared__ unsigned int red_prov[NW];
@@ -190,7 +208,6 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __shared__ unsigned int edge_fill;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t tile = p.tile_base + blockIdx.x;
   const TileGeo g = tile_geo(p, tile);
   const uint32_t utile = (uint32_t)tile;  // tile ids and node ids fit 32 bits
   const uint32_t node0 = utile * (uint32_t)kTV;
@@ -198,7 +215,13 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   const uint32_t lt = (1u << lane) - 1u;
   const int llim = limit_of(p.budget, kLocalLimit);
 
-  auto box_row_of = [&](int ri) -> int { return (ri / TY + HZ) * BY + (ri % TY) + 1; };
+  auto rb_of = [&](int ri) -> int { return (ri / TY + HZ) * BY + (ri % TY) + 1; };
+  // box row of halo row h: the whole first plane in 3D, then the two y faces
+  // of every tile plane
+  auto halo_rb = [&](int h) -> int {
+    const int q = h - HZ * BY;
+    return q < 0 ? h : (HZ + (q >> 1)) * BY + ((q & 1) ? BY - 1 : 0);
+  };
   auto at = [&](int rb, int x) -> T { return box[rb * W + PADX + x]; };
   // relation of a foreground voxel with value a and a neighbour b
   auto R = [&](T a, T b) -> bool {
@@ -212,7 +235,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     return dy + BY * dz;
   };
 
-  // ---- phase 0: the box arrives while the row tables are set up
+  // ---- phase 0: the box arrives while the node bases are set up
   if (tid == 0) {
     local_err = 0;
     edge_fill = 0;
@@ -221,7 +244,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       fence_mbar_init();
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&tbar, (uint32_t)(NRB * W * sizeof(T)));
-      tma_load_3d(box, &tmap, &tbar, (int)(x0 - PADX), (int)(y0 - 1), (int)(z0 - HZ));
+      tma_load_3d(box, tmap, &tbar, (int)(x0 - PADX), (int)(y0 - 1), (int)(z0 - HZ));
     }
   }
   if (!use_tma) {
@@ -245,37 +268,30 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       }
     }
   }
-  for (int rb = tid; rb < NRB; rb += kThreads) {
-    const int by = rb % BY, bz = rb / BY;
+  if (tid < NRB) {
+    const int rb = tid, by = rb % BY, bz = rb / BY;
     const bool trow = by >= 1 && by <= TY && bz >= HZ;
-    const int ty_off = by == 0 ? -1 : (by == BY - 1 ? 1 : 0);
-    const int tz_off = bz < HZ ? -1 : 0;
+    const int hidx = bz < HZ ? by : HZ * BY + (bz - HZ) * 2 + (by == 0 ? 0 : 1);
+    nbase[rb] = (unsigned short)(trow ? ((bz - HZ) * TY + by - 1) * 32 : HNODE + hidx * 32);
+    const int dy = by == 0 ? -1 : (by == BY - 1 ? 1 : 0);
+    const int dz = bz < HZ ? -1 : 0;
     const int ly = by == 0 ? TY - 1 : (by == BY - 1 ? 0 : by - 1);
     const int lz = bz < HZ ? TZ - 1 : bz - HZ;
+    rloc[rb] = (unsigned char)(ly + TY * lz);
+    // (rows outside the volume hold no foreground, so their tile id is unused)
+    rtile[rb] = utile + (uint32_t)dy * (uint32_t)g.ntx + (uint32_t)dz * ((uint32_t)g.ntx * (uint32_t)g.nty);
     // which tile holds a box row: its y and z offsets from this tile
     auto owner = [&](int r) -> int {
       const int b = r % BY, c = r / BY;
       return (b == 0 ? 0 : (b == BY - 1 ? 2 : 1)) + 3 * (c < HZ ? 0 : 1);
     };
-    const int own = (ty_off + 1) + 3 * (tz_off + 1);
+    const int own = (dy + 1) + 3 * (dz + 1);
     int prev = 255;
     if (by > 0 && owner(rb - 1) == own) prev = rb - 1;
     else if (bz > 0 && owner(rb - BY) == own) prev = rb - BY;
-    const int64_t y = y0 - 1 + by, z = z0 - HZ + bz;
-    const bool in_vol = y >= 0 && y < g.sy && z >= 0 && z < g.sz;
-    // halo rows: the whole first plane in 3D, then the two y faces of every
-    // tile plane
-    const int hidx = bz < HZ ? by : HZ * BY + (bz - HZ) * 2 + (by == 0 ? 0 : 1);
-    nbase[rb] = (unsigned short)(trow ? (ly + TY * lz) * 32 : HNODE + hidx * 32);
-    rloc[rb] = (unsigned short)(ly + TY * lz);
-    // (rows outside the volume hold no foreground, so their tile id is unused)
-    rtile[rb] = (uint32_t)(g.tile0 + g.tx + (int64_t)g.ntx * ((g.ty + ty_off) + (int64_t)g.nty * (g.tz + tz_off)));
-    rgrow[rb] = in_vol ? (uint32_t)(y + g.sy * z) : 0u;
     rprev[rb] = (unsigned char)prev;
-    rflag[rb] = (unsigned char)((trow ? 1 : 0) | (in_vol ? 2 : 0));
-    par[CNODE + rb] = (PT)(CNODE + rb);
-    par[CNODE + NRB + rb] = (PT)(CNODE + NRB + rb);
   }
+  if (tid < 2 * NRB) par[CNODE + tid] = (PT)(CNODE + tid);
   if (use_tma) {
     __syncthreads();  // the barrier is initialised before anyone polls it
     if (!mbar_wait_bounded(&tbar, 0)) {
@@ -285,41 +301,53 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   }
   __syncthreads();
 
-  // ---- phase 1: run masks of every box row; the run heads become nodes
+  // ---- phase A: run masks of every box row; run heads become nodes; the
+  // provisional-label estimate (cc3d/cc3d.hpp:287-315) on the tile rows
   unsigned long long epl_acc = 0;
-  int frb = -1, lrb = -1;  // first / last box rows with estimate transitions
-  for (int rb = warp; rb < NRB; rb += NW) {
+  int frb = NRB, lrb = -1;  // first / last box rows with estimate transitions
+  auto masks = [&](int rb, uint32_t& F, uint32_t& E) {
     const T v = at(rb, lane), vl = at(rb, lane - 1);
     const bool fg = v != T(0);
     // a voxel whose left neighbour (the real one, also across the x seam)
     // does not relate to it
     const bool diff = (MODE == MODE_MULTI) ? (v != vl) : (vl == T(0));
-    const uint32_t F = __ballot_sync(FULL, fg);
-    const uint32_t E = __ballot_sync(FULL, fg && diff);
+    F = __ballot_sync(FULL, fg);
+    E = __ballot_sync(FULL, fg && diff);
     const uint32_t S = E | (F & 1u);  // runs are cut at the tile's x seam
-    if (lane == 0) {
-      fmask[rb] = F;
-      smask[rb] = S;
-    }
-    if ((S >> lane) & 1u) {
-      const uint32_t n = nbase[rb] + lane;
-      par[n] = (PT)n;
-    }
-    if (MODE == MODE_MULTI && E && (rflag[rb] & 1u)) {
+    fmask[rb] = F;
+    smask[rb] = S;
+    return S;
+  };
+#pragma unroll 2
+  for (int j = 0; j < RPW; ++j) {
+    const int ri = warp_row<TY>(warp, j), rb = rb_of(ri);
+    uint32_t F, E;
+    const uint32_t S = masks(rb, F, E);
+    if ((S >> lane) & 1u) par[ri * 32 + lane] = (PT)(ri * 32 + lane);
+    if (MODE == MODE_MULTI && E) {
       epl_acc += __popc(E);
-      if (frb < 0) frb = rb;
-      lrb = rb;
+      frb = rb < frb ? rb : frb;
+      lrb = rb > lrb ? rb : lrb;
     }
+  }
+  for (int h = warp; h < NHR; h += NW) {
+    const int rb = halo_rb(h);
+    uint32_t F, E;
+    const uint32_t S = masks(rb, F, E);
+    if ((S >> lane) & 1u) par[HNODE + h * 32 + lane] = (PT)(HNODE + h * 32 + lane);
   }
   __syncthreads();
 
-  // ---- phase 2a: row-level relations.  The first pair of every run with
-  // its link row becomes a direct parent link (to a smaller node, so roots
-  // stay the smallest node of their tree); the other row-level pairs and the
-  // needy voxels go to the warp's list.
+  // ---- phase B: row-level relations and unions, warp by warp.  The first
+  // pair of every run with its link row becomes a direct parent link (to a
+  // smaller node, so roots stay the smallest node of their tree; by CAS, as
+  // other warps' unions may already have linked the run); where the link row
+  // is a halo row, each halo run's first pair links the halo run under the
+  // tile run instead.  The other row-level pairs and the needy voxels go to
+  // the warp's list, whose unions run once its rows are done.
   if (warp == 0) {
     // exclusive prefix of the run counts over the tile rows (two per lane)
-    const uint32_t a0 = __popc(smask[box_row_of(2 * lane)]), a1 = __popc(smask[box_row_of(2 * lane + 1)]);
+    const uint32_t a0 = __popc(smask[rb_of(2 * lane)]), a1 = __popc(smask[rb_of(2 * lane + 1)]);
     uint32_t sa = a0 + a1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -332,8 +360,8 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   }
   int un = 0;  // warp-uniform list fill
   unsigned short* ul = ulist[warp];
-  for (int ri = warp; ri < NR; ri += NW) {
-    const int rb = box_row_of(ri);
+  for (int j = 0; j < RPW; ++j) {
+    const int ri = warp_row<TY>(warp, j), rb = rb_of(ri);
     const int rl = rb + LOFF;
     const T v = at(rb, lane);
     const uint32_t F = fmask[rb], Sc = smask[rb], Sl = smask[rl];
@@ -358,23 +386,42 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     }
     if ((P >> lane) & 1u) {
       const int hx = head_of(Sc, lane);
-      const bool first = (P & lt & ~((1u << hx) - 1u)) == 0u;
-      if (first && ri >= LROW0) par[ri * 32 + hx] = (PT)(nbase[rl] + head_of(Sl, lane));
-      else km |= 2u;
+      const uint32_t h = (uint32_t)(ri * 32 + hx);
+      if (ri >= LROW0) {
+        // this run's first pair: parent = the link row's run
+        if ((P & lt & ~((1u << hx) - 1u)) == 0u) {
+          // the link row's run, or already its parent: the link row is
+          // normally one of this warp's earlier rows, whose runs point down
+          // their column, so every run of a column points at its bottom run
+          const uint32_t tl = (uint32_t)((ri - LSTEP) * 32 + head_of(Sl, lane));
+          const uint32_t t = ((const volatile PT*)par)[tl];
+          if ((uint32_t)atomicCAS(&par[h], (PT)h, (PT)t) != h) km |= 2u;
+        } else {
+          km |= 2u;
+        }
+      } else {
+        // the halo run's first pair: the halo run's parent = this run
+        const int hl = head_of(Sl, lane);
+        if ((P & lt & ~((1u << hl) - 1u)) == 0u) {
+          const uint32_t hn = (uint32_t)(nbase[rl] + hl);
+          if ((uint32_t)atomicCAS(&par[hn], (PT)hn, (PT)h) != hn) km |= 2u;
+        } else {
+          km |= 2u;
+        }
+      }
     }
     const unsigned need = (NEED >> lane) & 1u;
     const uint32_t Q = __ballot_sync(FULL, (km | need) != 0u);
     if ((Q >> lane) & 1u) ul[un + __popc(Q & lt)] = (unsigned short)((need << 14) | (km << 11) | (ri << 5) | lane);
     un += __popc(Q);
   }
-  __syncthreads();  // every direct link is in place before any union
+  __syncwarp();
 
-  // ---- phase 2b: the warp's list, one entry per lane: its union pairs are
-  // found first (the needy voxels' relation tests), collected, and run in
-  // dense rounds of one union per lane.  Bits of a lane's pair set: j < NB a
-  // needy voxel's relation j; NB the column x0 - 1 of its row; NB + 1 the
-  // row-level pair with the row behind (6); NB + 2 the row-level pair with
-  // the link row.
+  // the warp's list, one entry per lane: its union pairs are found first (the
+  // needy voxels' relation tests), collected, and run in dense rounds of one
+  // union per lane.  Bits of a lane's pair set: j < NB a needy voxel's
+  // relation j; NB the column x0 - 1 of its row; NB + 1 the row-level pair
+  // with the row behind (6); NB + 2 the row-level pair with the link row.
   int err = 0;
   int pc = 0;  // warp-uniform pair fill
   uint32_t* pw = pairs[warp];
@@ -399,7 +446,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       x = (int)(e & 31u);
       const int ri = (int)((e >> 5) & 63u);
       const unsigned km = (e >> 11) & 7u;
-      rb = box_row_of(ri);
+      rb = rb_of(ri);
       const uint32_t Sc = smask[rb];
       h = (unsigned short)(ri * 32 + head_of(Sc, x));
       m = ((km & 4u) ? 1u << NB : 0u) | ((km & 1u) ? 2u << NB : 0u) | ((km & 2u) ? 4u << NB : 0u);
@@ -457,21 +504,26 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   if (err) local_err = 1;
   __syncthreads();
 
-  // ---- phase 3: roots, run records, keys, bitmap.  A component is named by
-  // its root run (the smallest node of its tree, its first run in raster
-  // order): the run's index in the tile's run order.  Halo heads are only
+  // ---- phase C: roots, run records, keys, bitmap, warp by warp from the
+  // bottom of its columns up.  A component is named by its root run (the
+  // smallest node of its tree, its first run in raster order): the run's
+  // index in the tile's run order.  Halo heads and the halo columns are only
   // pointed at their roots, for the edges below.
   const uint32_t C = rbase[NR];
   auto rid_of = [&](unsigned r) -> unsigned {
-    return rbase[r >> 5] + __popc(smask[box_row_of((int)(r >> 5))] & ((1u << (r & 31u)) - 1u));
+    return rbase[r >> 5] + __popc(smask[rb_of((int)(r >> 5))] & ((1u << (r & 31u)) - 1u));
   };
-  const uint32_t wpr = (uint32_t)g.wpr, word0 = (uint32_t)g.word0, tx = (uint32_t)g.tx;
-  for (int rb = warp; rb < NRB; rb += NW) {
+  const uint32_t wpr = (uint32_t)g.wpr, tx = (uint32_t)g.tx;
+  const uint32_t sy32 = (uint32_t)g.sy;
+  // bitmap word of the tile's row (ly, lz) = bw0 + (lz * sy + ly) * wpr
+  const uint32_t bw0 = (uint32_t)g.word0 + ((uint32_t)z0 * sy32 + (uint32_t)y0) * wpr + tx;
+  for (int j = 0; j < RPW; ++j) {
+    const int ri = warp_row<TY>(warp, j), rb = rb_of(ri);
     const uint32_t S = smask[rb];
     bool root = false;
     uint32_t r = 0;
     if ((S >> lane) & 1u) {
-      const uint32_t n = nbase[rb] + lane;
+      const uint32_t n = (uint32_t)(ri * 32 + lane);
       r = lfind_ro<PT>(par, n, llim);
       if (par[r] != r) {
         // the find ran out of budget: the run becomes a root of its own (the
@@ -481,25 +533,29 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
       }
       par[n] = (PT)r;
       root = r == n;
-    }
-    if (!(rflag[rb] & 1u)) continue;
-    const int ri = rloc[rb];
-    const uint32_t bw = word0 + rgrow[rb] * wpr + tx;  // bitmap word of the row
-    if ((S >> lane) & 1u) {
       const unsigned c = rid_of(r);
       p.rcomp[node0 + rbase[ri] + __popc(S & lt)] = (uint16_t)c;
-      if (root) p.E[node0 + c] = ((unsigned long long)(bw * 32u + (uint32_t)lane) << 32) | (node0 + c);
+      if (root) {
+        const uint32_t bw = bw0 + ((uint32_t)(ri / TY) * sy32 + (uint32_t)(ri % TY)) * wpr;
+        p.E[node0 + c] = ((unsigned long long)(bw * 32u + (uint32_t)lane) << 32) | (node0 + c);
+      }
     }
-    const uint32_t rm = __ballot_sync(FULL, root);
-    if (lane == 0) {
-      const uint32_t rr = utile * (uint32_t)kRowsPerTile + (uint32_t)ri;
-      p.rmask[rr] = make_uint2(fmask[rb], S);
-      p.rrow[rr] = rbase[ri];
-      if (rflag[rb] & 2u) p.bitmap[bw] = rm;
+    rootm[ri] = __ballot_sync(FULL, root);
+  }
+  for (int h = warp; h < NHR; h += NW) {
+    const uint32_t S = smask[halo_rb(h)];
+    if ((S >> lane) & 1u) {
+      const uint32_t n = (uint32_t)(HNODE + h * 32 + lane);
+      uint32_t r = lfind_ro<PT>(par, n, llim);
+      if (par[r] != r) {
+        local_err = 1;
+        r = n;
+      }
+      par[n] = (PT)r;
     }
   }
-  for (int c = tid; c < 2 * NRB; c += kThreads) {
-    const uint32_t n = (uint32_t)(CNODE + c);
+  if (tid < 2 * NRB) {
+    const uint32_t n = (uint32_t)(CNODE + tid);
     uint32_t r = lfind_ro<PT>(par, n, llim);
     if (par[r] != r) {
       local_err = 1;
@@ -507,9 +563,20 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     }
     par[n] = (PT)r;
   }
+  __syncwarp();
+  // the row records of the warp's rows, one lane per row
+  if (lane < RPW) {
+    const int ri = warp_row<TY>(warp, lane), rb = rb_of(ri);
+    const uint32_t rr = utile * (uint32_t)kRowsPerTile + (uint32_t)ri;
+    p.rmask[rr] = make_uint2(fmask[rb], smask[rb]);
+    p.rrow[rr] = rbase[ri];
+    const int ly = ri % TY, lz = ri / TY;
+    if (y0 + ly < g.sy && z0 + lz < g.sz)
+      p.bitmap[bw0 + ((uint32_t)lz * sy32 + (uint32_t)ly) * wpr] = rootm[ri];
+  }
   __syncthreads();
 
-  // ---- phase 4: one edge per halo run / halo-column voxel joined to a tile
+  // ---- phase D: one edge per halo run / halo-column voxel joined to a tile
   // component, except where the same-owner voxel just before it (one row back
   // in y, else in z) relates to it and joined the same component: both lie
   // in one component of their own tile, so that edge would repeat
@@ -519,12 +586,9 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
     bool has = false;
     uint2 e = make_uint2(0u, 0u);
     if (it < NHR) {
-      // halo row `it`: the whole first plane in 3D, then the two y faces of
-      // every tile plane
-      const int q = it - HZ * BY;
-      const int rb = q < 0 ? it : (HZ + (q >> 1)) * BY + ((q & 1) ? BY - 1 : 0);
+      const int rb = halo_rb(it);
       if ((smask[rb] >> lane) & 1u) {  // run heads stand for their runs
-        const uint32_t r = par[nbase[rb] + lane];
+        const uint32_t r = par[HNODE + it * 32 + lane];
         if (r < kTV) {
           has = true;
           const int rp = rprev[rb];
@@ -578,7 +642,7 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   if (MODE == MODE_BINARY && p.want_prov) {
     auto colfg = [&](int rb, int xi) -> uint32_t { return at(rb, xi) != T(0) ? 1u : 0u; };
     for (int ri = warp; ri < NR; ri += NW) {
-      const int rb = box_row_of(ri);
+      const int rb = rb_of(ri);
       const uint32_t F = fmask[rb];
       uint32_t Lk = (F << 1) | colfg(rb, -1);
 #pragma unroll
@@ -606,27 +670,36 @@ k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) 
   __syncthreads();
   if (tid == 0) {
     unsigned long long e = 0, pv = 0;
-    int f = -1, l = -1;
+    int f = NRB, l = -1;
     for (int w = 0; w < NW; ++w) {
       e += red_epl[w];
       pv += red_prov[w];
       // box-row order is raster order for rows inside the volume
-      if (red_first[w] >= 0 && (f < 0 || red_first[w] < f)) f = red_first[w];
-      if (red_last[w] > l) l = red_last[w];
+      f = red_first[w] < f ? red_first[w] : f;
+      l = red_last[w] > l ? red_last[w] : l;
     }
+    auto grow = [&](int rb) -> long long {
+      return (long long)(y0 - 1 + rb % BY) + (long long)g.sy * (long long)(z0 - HZ + rb / BY);
+    };
     const uint32_t nedges = edge_fill;
     TileInfo ti;
     ti.C = C;
     ti.nedges = nedges < p.edge_slots ? nedges : p.edge_slots;
     ti.epl = (uint32_t)e;
     ti.prov = (uint32_t)pv;
-    ti.first_row = f >= 0 ? (long long)rgrow[f] : 0x7FFFFFFFFFFFFFFFLL;
-    ti.last_row = l >= 0 ? (long long)rgrow[l] : -1;
+    ti.first_row = f < NRB ? grow(f) : 0x7FFFFFFFFFFFFFFFLL;
+    ti.last_row = l >= 0 ? grow(l) : -1;
     p.tinfo[tile] = ti;
     if (nedges > p.edge_slots) atomicOr(&p.ctr->err, ERR_EDGE_OVERFLOW);
     if (local_err)
       atomicOr(&p.ctr->err, local_err == 3 ? ERR_WAIT : (local_err == 2 ? ERR_INDEX : ERR_LOCAL_BUDGET));
   }
+}
+
+template <typename T, int CONN, int TY, int TZ, int MODE>
+__global__ void __launch_bounds__(kThreads, 6)
+k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
+  tile_list_tile<T, CONN, TY, TZ, MODE>(p, &tmap, use_tma, p.tile_base + blockIdx.x);
 }
 
 }  // namespace cc3dgpu

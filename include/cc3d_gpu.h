@@ -426,10 +426,7 @@ int cc3d_gpu_cost_model_choose(const void* in, int dtype, int64_t sx, int64_t sy
                                float min_margin, int* choice, int* confident);
 
 /*
- * Batches: many volumes labelled by one launch of each stage, the stage
- * sequence captured once into a CUDA graph per batch layout (dtype,
- * connectivity, tile-pass configuration and the list of shapes) and replayed
- * while the layout repeats.  No counterpart in the reference, whose callers
+ * Batches: many volumes labelled together.  No counterpart in the reference, whose callers
  * loop over cc3d.connected_components (the result of every volume is
  * identical to that call's: labels, N, and the output type the Cython layer
  * would choose, cc3d/fastcc3d.pyx:388-434).
@@ -461,6 +458,22 @@ typedef struct {
 
 int cc3d_gpu_label_batch(const cc3d_gpu_volume* volumes, int n, int dtype, int64_t connectivity,
                          cc3d_gpu_volume_result* results, void* stream);
+/* How this thread's cc3d_gpu_label_batch runs (returns the previous mode):
+ *   CC3D_BATCH_PERSISTENT (the default): ONE cooperative kernel launch walks
+ *     every stage over the whole batch (tile pass, edge merges, numbering
+ *     scan, per-volume results, labels) with bounded grid barriers between
+ *     stages; its arguments come from a header uploaded to device memory, so
+ *     the launch is captured into a CUDA graph once (per kernel, grid and
+ *     workspace) and replayed for batches of any layout.  3D volumes use the
+ *     list pass on 32 x 8 x 8 tiles, 2D images 32 x 64.
+ *   CC3D_BATCH_STAGED: one launch per stage (the tile-pass configuration from
+ *     the autotuner), the stage sequence captured into a CUDA graph per batch
+ *     layout (dtype, connectivity, configuration, list of shapes) and replayed
+ *     while the layout repeats.
+ * cc3d_gpu_autotune_batch times the staged configurations. */
+#define CC3D_BATCH_PERSISTENT 0
+#define CC3D_BATCH_STAGED 1
+int cc3d_gpu_set_batch_mode(int mode);
 /* Release this thread's batch workspace and graphs. */
 void cc3d_gpu_release_batch(void);
 /* Time every tile-pass configuration on this batch (2D: the first two; best

@@ -1,7 +1,8 @@
 """Batches (cc3d_gpu_label_batch): every volume of a batch gets exactly what
 the single-volume path gives it -- labels, N and output dtype -- and the
-oracle agrees.  A repeated list of shapes replays the captured graph with new
-buffers and data."""
+oracle agrees, in both batch modes (one persistent launch; one launch per
+stage).  A repeated list of shapes replays the captured graph with new
+buffers and data; the persistent launch replays its graph for any list."""
 import numpy as np
 import pytest
 
@@ -11,12 +12,15 @@ import __graft_entry__ as entry
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def cc3d():
+@pytest.fixture(scope="module", params=["persistent", "staged"])
+def cc3d(request):
     entry.build()
     import torch
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
-    return entry.package()
+    pkg = entry.package()
+    prev = pkg.set_batch_mode(request.param)
+    yield pkg
+    pkg.set_batch_mode(prev)
 
 
 def _shapes(rng, n, lo, hi, dims=3):
@@ -90,3 +94,28 @@ def test_autotune_batch_records_a_choice(cc3d):
     assert res["best"] in CONFIGS and set(res["ms"]) == set(CONFIGS)
     assert all(v > 0 for v in res["ms"].values())
     _check_batch(cc3d, vols, 26, n_oracle=1)
+
+
+def test_persistent_replays_for_new_layouts(cc3d):
+    # every call a different list of shapes (new layout): the persistent mode
+    # keeps one graph, the staged mode captures a new one each time
+    rng = np.random.default_rng(11)
+    for seed in (6, 7, 8):
+        vols = _voronoi_batch(_shapes(rng, 10 + seed, 16, 72), seed=seed)
+        _check_batch(cc3d, vols, 26, n_oracle=1)
+
+
+def test_both_modes_agree_on_a_mixed_stream():
+    entry.build()
+    pkg = entry.package()
+    rng = np.random.default_rng(12)
+    vols = _voronoi_batch(_shapes(rng, 64, 16, 128), seed=9)
+    prev = pkg.set_batch_mode("persistent")
+    try:
+        a = pkg.connected_components_batch(vols, connectivity=26, return_N=True)
+        pkg.set_batch_mode("staged")
+        b = pkg.connected_components_batch(vols, connectivity=26, return_N=True)
+    finally:
+        pkg.set_batch_mode(prev)
+    for (la, na), (lb, nb) in zip(a, b):
+        assert na == nb and la.dtype == lb.dtype and np.array_equal(la.cpu().numpy(), lb.cpu().numpy())
