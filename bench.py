@@ -442,10 +442,12 @@ def run_gpu(args, world, rank, local):
     if world == 1 and not args.skip_cpu:
         cpu = cpu_reference(vol)
 
-    # the mixed-size stream: batched vs the plain per-volume path
+    # the mixed-size stream: batched vs the plain per-volume path, and the
+    # shipped cost model's regret on a held-out stream
     batch = None
     if world == 1 and not args.skip_batch:
         batch = measure_batch(batch_stream(BATCH_VOLUMES), max(3, min(args.steps, 10)), 3)
+        batch["costmodel"] = costmodel_regret()
 
     launches_per_step = 8  # tile pass, edge merge, 3 scan kernels + tile reduction, resolve, write
     line = {
@@ -708,28 +710,54 @@ def batch_stream(n: int):
 
 def measure_batch(vols, steps: int, warmup: int) -> dict:
     """The batched path against the plain per-volume path on the same stream,
-    26-connectivity, device-resident inputs.
+    26-connectivity, device-resident inputs, both through the C ABI with
+    outputs allocated beforehand.
 
-    batched   cc3d.connected_components_batch, tile pass from the batch
-              autotuner; every timed step labels the stream in a fresh
-              random order, so each step is a new batch layout and its CUDA
-              graph is captured inside the timed region.
+    batched   cc3d_gpu_label_batch in the persistent mode (one cooperative
+              kernel launch per batch, replayed from a CUDA graph); every
+              timed step labels the stream in a fresh random order, so each
+              step is a new batch layout.
+    staged    the same calls in the staged mode (one launch per stage, the
+              tuned tile pass; its graph is captured per layout, inside the
+              timed region).
+    api       cc3d.connected_components_batch (persistent), which also builds
+              the descriptors and the per-volume output tensors in Python.
     per volume  one cc3d_gpu_label_prepare + cc3d_gpu_label_finish per volume
-              through the C ABI (ctypes, device buffers, outputs allocated
-              beforehand), one tile-pass configuration (list/8x8) for all.
+              (ctypes, device buffers), one tile-pass configuration
+              (list/8x8) for all.
     Every volume's batched labels, N and dtype are checked against its
     per-volume result."""
     import torch
     import cc3d_gb300 as cc3d
+    from cc3d_gb300 import batch as cbatch
     nat = cc3d._native
     lib = nat.load()
     voxels = int(sum(v.size for v in vols))
     dev = [torch.from_numpy(v).cuda() for v in vols]
+    n = len(dev)
     tuned = cc3d.autotune_batch(dev, connectivity=26)
     rng = np.random.default_rng(5)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # one output pool, 4 bytes per voxel, 256-byte aligned slices
+    sizes = [((d.numel() * 4 + 255) // 256) * 256 for d in dev]
+    pool = torch.empty((sum(sizes),), dtype=torch.uint8, device="cuda")
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    shapes = np.array([d.shape for d in dev], np.int64)
+    ins = np.array([d.data_ptr() for d in dev], np.uint64)
+    res = np.zeros(n, cbatch._RESULT_DTYPE)
+
+    def abi_batch(order):
+        desc = np.empty(n, cbatch._VOLUME_DTYPE)
+        desc["in"] = ins[order]
+        desc["out"] = pool.data_ptr() + offs[order]
+        desc["sx"], desc["sy"], desc["sz"] = shapes[order, 2], shapes[order, 1], shapes[order, 0]
+        nat.check(lib.cc3d_gpu_label_batch(desc.ctypes.data, n, nat.U16, 26, res.ctypes.data, stream))
 
     def batched():
-        order = rng.permutation(len(dev))
+        abi_batch(rng.permutation(n))
+
+    def api():
+        order = rng.permutation(n)
         return cc3d.connected_components_batch([dev[i] for i in order], connectivity=26, return_N=True)
 
     def timed(fn, k):
@@ -745,51 +773,60 @@ def measure_batch(vols, steps: int, warmup: int) -> dict:
         torch.cuda.synchronize()
         return max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3) / k
 
-    ms_batch = timed(batched, steps)
-    # the same stream through the staged batcher (one launch per stage, its
-    # graph captured per layout: every step is a new layout)
-    prev_mode = cc3d.set_batch_mode("staged")
+    prev_mode = cc3d.set_batch_mode("persistent")
     try:
+        ms_batch = timed(batched, steps)
+        ms_api = timed(api, steps)
+        cc3d.set_batch_mode("staged")
         ms_staged = timed(batched, steps)
     finally:
         cc3d.set_batch_mode(prev_mode)
     # the plain path: per-volume C ABI calls, preallocated uint32 outputs
     outs = [torch.empty(d.shape, dtype=torch.uint32, device="cuda") for d in dev]
-    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     flags = nat.IN_DEVICE | nat.OUT_DEVICE
     prev = cc3d.set_tile_pass("list/8x8")
 
     def plain():
-        res = []
+        out = []
         for d, o in zip(dev, outs):
             sz, sy, sx = d.shape
             info = nat.Prepared()
             nat.check(lib.cc3d_gpu_label_prepare(d.data_ptr(), nat.U16, sx, sy, sz, 26, 0, 0, flags, stream,
                                                  ctypes.byref(info)))
-            n = ctypes.c_uint64(0)
+            nn = ctypes.c_uint64(0)
             code = nat.U16 if min(info.epl, d.numel()) < 65535 else nat.U32
             nat.check(lib.cc3d_gpu_label_finish(info.token, int(min(info.epl, d.numel())), o.data_ptr(), code,
-                                                ctypes.byref(n), flags, stream))
-            res.append((n.value, code))
-        return res
+                                                ctypes.byref(nn), flags, stream))
+            out.append((nn.value, code))
+        return out
 
     try:
         ms_plain = timed(plain, max(1, steps // 2))
         plain_res = plain()
     finally:
         cc3d.set_tile_pass(prev)
-    got = cc3d.connected_components_batch(dev, connectivity=26, return_N=True)
+    # the persistent batch in stream order, checked volume by volume
+    prev_mode = cc3d.set_batch_mode("persistent")
+    try:
+        abi_batch(np.arange(n))
+        torch.cuda.synchronize()
+    finally:
+        cc3d.set_batch_mode(prev_mode)
     mismatches = 0
-    for (lab, n), (pn, pcode), o in zip(got, plain_res, outs):
-        pdt = torch.uint16 if pcode == nat.U16 else torch.uint32
-        ref = o.view(-1)[:lab.numel()].view(pdt).view(lab.shape) if pdt == torch.uint32 else \
-            o.view(torch.uint16).view(-1)[:lab.numel()].view(lab.shape)
-        mismatches += int(pn != n or lab.dtype != pdt or not torch.equal(ref.to(torch.int64), lab.to(torch.int64)))
+    out_bytes = 0
+    for i, ((pn, pcode), o, d) in enumerate(zip(plain_res, outs, dev)):
+        code, N = int(res["out_dtype"][i]), int(res["N"][i])
+        w = 2 if code == nat.U16 else 4
+        out_bytes += w * d.numel()
+        got = pool[offs[i]:offs[i] + w * d.numel()]
+        ref = o.view(torch.uint8)[:w * d.numel()]  # (a uint16 result fills the buffer's first half)
+        mismatches += int(pn != N or code != pcode or not torch.equal(got, ref))
     peak, peak_kind = load_peaks()
-    out_bytes = sum(o.element_size() * o.numel() for o in (lab for lab, _ in got))
     alg_bytes = voxels * 2 + out_bytes
     gbs = alg_bytes / (ms_batch / 1e3) / 1e9
     return {"value": voxels / ms_batch / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_batch,
+            "path": "cc3d_gpu_label_batch, persistent mode: one cooperative kernel launch per batch, "
+                    "replayed from a CUDA graph (C ABI, device buffers, outputs allocated beforehand)",
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "peak_source": peak_kind, "algorithmic_bytes_per_step": alg_bytes},
             "per_volume": {"value": voxels / ms_plain / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_plain,
@@ -797,12 +834,15 @@ def measure_batch(vols, steps: int, warmup: int) -> dict:
                                    "device buffers), tile pass list/8x8 for every volume"},
             "ratio_batched_vs_per_volume": ms_plain / ms_batch,
             "staged": {"value": voxels / ms_staged / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_staged,
-                       "path": "one launch per stage, the stage graph captured per layout (tuned tile pass)"},
-            "mode": "persistent: one cooperative kernel launch per batch, replayed from a CUDA graph",
+                       "path": "cc3d_gpu_label_batch, staged mode: one launch per stage, the stage graph "
+                               "captured per layout (tuned tile pass)"},
+            "api": {"value": voxels / ms_api / 1e6, "unit": "GVoxels/s", "ms_per_step": ms_api,
+                    "path": "cc3d.connected_components_batch (persistent), descriptors and output tensors "
+                            "built in Python every step"},
             "mismatched_volumes": mismatches, "tuned": tuned,
             "workload": f"{len(vols)} uint16 Voronoi+membrane volumes, edges log-uniform in [16, 256], one seed "
                         "per 4096 voxels, connectivity 26, device-resident; each timed batched step in a "
-                        "fresh volume order (a new layout: its graph capture is timed)",
+                        "fresh volume order (a new layout)",
             "voxels": voxels}
 
 
@@ -840,10 +880,31 @@ def run_batch(args):
 
 
 # ------------------------------------------------------------ cost model
+COSTMODEL_HELD_OUT = 40  # volumes of the held-out stream timed by the default run
+
+
+def costmodel_regret() -> dict:
+    """The shipped cost model (cc3d_gb300/costmodel_params.npy) judged on a
+    held-out-seed stream of COSTMODEL_HELD_OUT generated volumes (edges 64-256,
+    the training generators): every configuration timed by the exhaustive
+    autotuner, the model's pick compared with the best and with the plain
+    single configuration (list/8x8)."""
+    import cc3d_gb300 as cc3d
+    cm = cc3d.costmodel
+    if not cm.load():
+        return {"unavailable": "no shipped parameters"}
+    t0 = time.perf_counter()
+    Xt, Yt, _ = cm.collect(COSTMODEL_HELD_OUT, seed=7, lo=64, hi=256, repeats=2)
+    reg = cm.regret(Yt, cm.predict(Xt))
+    reg.update({"volumes": int(Xt.shape[0]), "timings": int(np.isfinite(Yt).sum()), "held_out_seed": 7,
+                "plain_config": "list/8x8", "seconds": time.perf_counter() - t0})
+    return reg
+
+
 def run_costmodel(args):
     """Train the cost model on autotuner timings of `args.costmodel` generated
     volumes (Voronoi with 1 to ~1e6 seeds, Bernoulli p 0.05-0.95, multilabel
-    Bernoulli K 2-1000; uint8/16/32/64; edges 64-320; connectivity 26/18/6)
+    Bernoulli K 2-1000; uint8/16/32/64; edges 64-768; connectivity 26/18/6)
     and evaluate it on a held-out-seed stream by its regret against the
     exhaustive autotuner.  One JSON line; the parameters are saved where
     --save-params says (and loaded by set_tile_pass("model") when shipped in
@@ -853,12 +914,12 @@ def run_costmodel(args):
     cm = cc3d.costmodel
     cc3d.build()
     t0 = time.perf_counter()
-    X, Y, _ = cm.collect(args.costmodel, seed=1, repeats=2)
+    X, Y, _ = cm.collect(args.costmodel, seed=1, lo=64, hi=768, repeats=2)
     t_collect = time.perf_counter() - t0
     loss = cm.train(X, Y, epochs=300, batch=256, lr=1e-3, seed=0)
     t_train = time.perf_counter() - t0 - t_collect
     n_test = max(50, args.costmodel // 5)
-    Xt, Yt, desc = cm.collect(n_test, seed=2, repeats=2)
+    Xt, Yt, desc = cm.collect(n_test, seed=2, lo=64, hi=768, repeats=2)
     P = cm.predict(Xt)
     reg = cm.regret(Yt, P)
     low_conf = reg["fallback_fraction"]
@@ -872,7 +933,9 @@ def run_costmodel(args):
         "train": {"volumes": int(X.shape[0]), "timings": int(np.isfinite(Y).sum()), "final_loss": loss,
                   "collect_s": t_collect, "train_s": t_train},
         "test": {"volumes": int(Xt.shape[0]), "timings": int(np.isfinite(Yt).sum())},
-        "model": "FP32 MLP 16-64-64-6 (ReLU), Adam, trained by the library's CUDA kernels",
+        "model": "FP32 MLP 16-64-64-12 (ReLU), Adam, trained by the library's CUDA kernels; outputs: "
+                 "log-ms of list/runs x 8x8/4x16/16x4 x TMA/plain-load box",
+        "plain_config": "list/8x8 (the default single configuration)",
     }), flush=True)
 
 

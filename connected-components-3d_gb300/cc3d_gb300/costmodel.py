@@ -1,5 +1,5 @@
 """The learned cost model (include/cc3d_gpu.h: cc3d_gpu_volume_features,
-cc3d_gpu_cost_model_*): an FP32 MLP 16 -> 64 -> 64 -> 6 that predicts the log
+cc3d_gpu_cost_model_*): an FP32 MLP 16 -> 64 -> 64 -> 12 that predicts the log
 milliseconds of every tile-pass configuration from features sampled on the
 device, trained on the autotuner's own timings.  Training and inference run in
 the library's CUDA kernels; this module generates the timing data, drives the
@@ -22,7 +22,7 @@ from .tuning import CONFIGS, _volume, config_name
 
 N_FEATURES = 16
 N_OUTPUTS = len(CONFIGS)
-N_PARAMS = 5682
+N_PARAMS = 6084
 DEFAULT_PARAMS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "costmodel_params.npy")
 
 
@@ -220,7 +220,7 @@ def regret(Y_true: np.ndarray, Y_pred: np.ndarray, min_margin: float = 0.05) -> 
     unsure = (srt[:, 1] - srt[:, 0]) < np.log1p(min_margin)
     picked_fb = np.where(unsure, best, picked)
     r_fb = np.exp(picked_fb - best) - 1.0
-    plain = true[:, 0]  # runs/8x8: the single default configuration
+    plain = true[:, 0]  # list/8x8: the single default configuration
     return {"mean_regret": float(r.mean()), "p95_regret": float(np.percentile(r, 95)),
             "top1": float((pick == true.argmin(axis=1)).mean()),
             "time_vs_best": float(np.exp(picked).sum() / np.exp(best).sum()),

@@ -21,18 +21,26 @@ VARIANTS = ("list", "runs")
 _VARIANT_BITS = {"runs": 1, "list": 2}
 SHAPES = ("8x8", "4x16", "16x4")   # 3D tiles 32 x TY x TZ; 2D images always use 32 x 64
 _SHAPE_BITS = {"8x8": 0x00, "4x16": 0x10, "16x4": 0x20}
+LOADS = ("", "plain")              # the box by one TMA copy, or by plain loads
+_PLAIN = 0x100
 # configuration index -> name, in the order of cc3d_gpu_tile_config
-CONFIGS = tuple(f"{v}/{s}" for s in SHAPES for v in VARIANTS)
+CONFIGS = tuple(f"{v}/{s}" + (f"/{ld}" if ld else "") for s in SHAPES for v in VARIANTS for ld in LOADS)
 
 
 def config_code(name: str) -> int:
-    """CC3D_TILE_* code of "auto", "model", "list", "runs" or "<variant>/<shape>"."""
+    """CC3D_TILE_* code of "auto", "model", "list", "runs" or
+    "<variant>/<shape>[/plain]"."""
     if name == "auto":
         return 0
     if name == "model":
         return 3
-    variant, _, shape = name.partition("/")
-    return _VARIANT_BITS[variant] | _SHAPE_BITS[shape or "8x8"]
+    parts = name.split("/")
+    code = _VARIANT_BITS[parts[0]] | _SHAPE_BITS[parts[1] if len(parts) > 1 else "8x8"]
+    if len(parts) > 2:
+        if parts[2] != "plain":
+            raise KeyError(name)
+        code |= _PLAIN
+    return code
 
 
 def config_name(code: int) -> str:
@@ -41,12 +49,13 @@ def config_name(code: int) -> str:
     if code == 3:
         return "model"
     variant = {b: v for v, b in _VARIANT_BITS.items()}[code & 15]
-    return f"{variant}/{SHAPES[(code >> 4) & 15]}"
+    return f"{variant}/{SHAPES[(code >> 4) & 15]}" + ("/plain" if code & _PLAIN else "")
 
 
 def set_tile_pass(name: str) -> str:
     """Select the calling thread's tile-pass configuration: "auto", "list",
-    "runs" (32x8x8 tiles) or "<variant>/<shape>" such as "runs/4x16".
+    "runs" (32x8x8 tiles) or "<variant>/<shape>[/plain]" such as "runs/4x16"
+    or "list/16x4/plain" (the tile's box by plain loads instead of TMA).
     "model" lets the learned cost model choose per volume (the parameters
     shipped with the package are loaded if no model was trained or loaded).
     Returns the previous setting."""

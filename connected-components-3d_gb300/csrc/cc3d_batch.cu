@@ -119,11 +119,14 @@ extern "C" int cc3d_gpu_autotune_batch(const cc3d_gpu_volume* vols, int n, int d
   if (!best) return failf(CC3D_ERR_INVALID, "invalid arguments");
   if (repeats < 1) repeats = 1;
   const bool d3 = connectivity == 26 || connectivity == 18 || connectivity == 6;
-  const int ncfg = d3 ? CC3D_TILE_CONFIGS : 2;
+  // (batches read their boxes with plain loads whatever the load-path bit
+  // says, so only the configurations without it are timed)
+  const int ncfg = d3 ? CC3D_TILE_CONFIGS : 4;
   double t[CC3D_TILE_CONFIGS];
   int bi = 0;
   for (int k = 0; k < CC3D_TILE_CONFIGS; ++k) t[k] = -1.0;
   for (int k = 0; k < ncfg; ++k) {
+    if (cc3d_gpu_tile_config(k) & CC3D_TILE_PLAIN) continue;
     t[k] = 1e300;
     for (int r = 0; r < repeats + 1; ++r) {
       const auto t0 = std::chrono::steady_clock::now();

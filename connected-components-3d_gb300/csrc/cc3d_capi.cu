@@ -263,11 +263,11 @@ int resolve_tile_pass(int dtype, int eff, int mode, int64_t voxels) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(dtype, eff, mode, size_bucket(voxels)));
   if (it != g_tuned.end()) return it->second;
-  // without tuning data: the list pass; 32 x 16 x 4 tiles for large
-  // volumes at 18/26-connectivity (fewer halo planes per voxel), 32 x 8 x 8
-  // otherwise (small volumes waste less of a 16-row tile)
-  return ((eff == 26 || eff == 18) && voxels >= (int64_t(1) << 24)) ? (CC3D_TILE_LIST | CC3D_TILE_16x4)
-                                                                    : CC3D_TILE_LIST;
+  // without tuning data: the list pass on 32 x 8 x 8 tiles, box by TMA
+  (void)eff;
+  (void)mode;
+  (void)voxels;
+  return CC3D_TILE_LIST;
 }
 }  // namespace
 
@@ -479,6 +479,7 @@ static int label_prepare(const void* in, int dtype, int64_t sx, int64_t sy, int6
   LabelArgs& a = job.args;
   memset(&a, 0, sizeof(a));
   a.budget = union_budget();
+  a.no_tma = cfg.plain ? 1 : 0;
   a.sx = sx; a.sy = sy; a.sz = sz;
   a.ntx = (int)((sx + kTX - 1) / kTX);
   a.nty = (int)((sy + TY - 1) / TY);
@@ -906,7 +907,7 @@ int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz, int
   const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
   if (binary_image && conn == 8) return CC3D_TILE_RUNS;
   int code = resolve_tile_pass(dtype, eff, mode, sx * sy * sz);
-  if (!(eff == 26 || eff == 18 || eff == 6)) code &= 15;  // 2D: one tile shape
+  if (!(eff == 26 || eff == 18 || eff == 6)) code &= ~0xF0;  // 2D: one tile shape
   return code;
 }
 
@@ -921,7 +922,7 @@ int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t
   if (sz == 1 && conn == 6) eff = 4;
   const bool d3 = eff == 26 || eff == 18 || eff == 6;
   const int mode = !binary_image ? MODE_MULTI : (conn == 4 ? MODE_BINARY4 : MODE_BINARY);
-  const int ncfg = d3 ? CC3D_TILE_CONFIGS : 2;
+  const int ncfg = d3 ? CC3D_TILE_CONFIGS : 4;  // 2D: the 8x8 entries (one tile shape)
   double t[CC3D_TILE_CONFIGS];
   int bi = 0;
   for (int k = 0; k < CC3D_TILE_CONFIGS; ++k) t[k] = -1.0;
@@ -953,9 +954,12 @@ int cc3d_gpu_autotune(const void* in, int dtype, int64_t sx, int64_t sy, int64_t
 
 int cc3d_gpu_tile_config(int index) {
   static const int codes[CC3D_TILE_CONFIGS] = {
-      CC3D_TILE_LIST | CC3D_TILE_8x8,  CC3D_TILE_RUNS | CC3D_TILE_8x8,
-      CC3D_TILE_LIST | CC3D_TILE_4x16, CC3D_TILE_RUNS | CC3D_TILE_4x16,
-      CC3D_TILE_LIST | CC3D_TILE_16x4, CC3D_TILE_RUNS | CC3D_TILE_16x4};
+      CC3D_TILE_LIST | CC3D_TILE_8x8,  CC3D_TILE_LIST | CC3D_TILE_8x8 | CC3D_TILE_PLAIN,
+      CC3D_TILE_RUNS | CC3D_TILE_8x8,  CC3D_TILE_RUNS | CC3D_TILE_8x8 | CC3D_TILE_PLAIN,
+      CC3D_TILE_LIST | CC3D_TILE_4x16, CC3D_TILE_LIST | CC3D_TILE_4x16 | CC3D_TILE_PLAIN,
+      CC3D_TILE_RUNS | CC3D_TILE_4x16, CC3D_TILE_RUNS | CC3D_TILE_4x16 | CC3D_TILE_PLAIN,
+      CC3D_TILE_LIST | CC3D_TILE_16x4, CC3D_TILE_LIST | CC3D_TILE_16x4 | CC3D_TILE_PLAIN,
+      CC3D_TILE_RUNS | CC3D_TILE_16x4, CC3D_TILE_RUNS | CC3D_TILE_16x4 | CC3D_TILE_PLAIN};
   if (index < 0 || index >= CC3D_TILE_CONFIGS) return -1;
   return codes[index];
 }

@@ -3,7 +3,7 @@
 // The cost model predicts, from 16 cheap features of a volume, the log of the
 // labelling time of every tile-pass configuration (CC3D_TILE_CONFIGS outputs),
 // so that a configuration can be chosen without timing them all.  It is a
-// small FP32 MLP, 16 -> 64 -> 64 -> 6 with ReLU, trained on timings the
+// small FP32 MLP, 16 -> 64 -> 64 -> 12 with ReLU, trained on timings the
 // autotuner itself produces.  Training (mini-batch Adam on a squared error
 // over the measured outputs) and inference are the kernels below; the
 // features are sampled on the device.  It never affects labels: every
@@ -24,7 +24,7 @@ namespace {
 
 constexpr int NF = CC3D_COST_FEATURES;  // 16
 constexpr int NH = 64;
-constexpr int NO = CC3D_TILE_CONFIGS;  // 6
+constexpr int NO = CC3D_TILE_CONFIGS;  // 12: variant x tile shape x load path
 // parameter layout: W1[NF][NH] b1[NH] W2[NH][NH] b2[NH] W3[NH][NO] b3[NO]
 constexpr int OW1 = 0, OB1 = OW1 + NF * NH, OW2 = OB1 + NH, OB2 = OW2 + NH * NH, OW3 = OB2 + NH,
               OB3 = OW3 + NH * NO, NPARAM = OB3 + NO;
@@ -487,7 +487,7 @@ extern "C" int cc3d_gpu_cost_model_choose(const void* in, int dtype, int64_t sx,
     return CC3D_OK;
   }
   const bool d3 = sz != 1 && (conn == 26 || conn == 18 || conn == 6);
-  const int ncfg = d3 ? NO : 2;
+  const int ncfg = d3 ? NO : 4;  // 2D: the 8x8 entries (one tile shape)
   float f[NF], y[NO];
   if (int rc = cc3d_gpu_volume_features(in, dtype, sx, sy, sz, connectivity, binary_image, mem_flags, stream, f))
     return rc;

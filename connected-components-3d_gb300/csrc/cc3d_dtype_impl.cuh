@@ -180,7 +180,7 @@ constexpr CUtensorMapDataType tma_type() {
 template <typename T>
 int encode_input_map(const LabelArgs& a, uint32_t bw, uint32_t bh, uint32_t bd, CUtensorMap* map) {
   memset(map, 0, sizeof(*map));
-  const bool aligned = !a.vols && ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
+  const bool aligned = !a.vols && !a.no_tma && ((uintptr_t)a.in & 15u) == 0 && (a.sx * (int64_t)sizeof(T)) % 16 == 0 &&
                        a.sx < (1ll << 31) && a.sy < (1ll << 31) && a.sz < (1ll << 31);
   if (!aligned) return 0;
   using Encode = decltype(&cuTensorMapEncodeTiled);

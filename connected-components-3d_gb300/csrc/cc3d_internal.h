@@ -20,16 +20,19 @@ constexpr int TILE_PASS_LIST = 2;
 
 // A tile-pass configuration (the CC3D_TILE_* codes of include/cc3d_gpu.h):
 // variant in bits 0-3, 3D tile shape in bits 4-7 (0: 32x8x8, 1: 32x4x16,
-// 2: 32x16x4).  2D images always use 32x64 tiles.
+// 2: 32x16x4), bit 8: the box by plain loads instead of one TMA copy.  2D
+// images always use 32x64 tiles.
 struct TileCfg {
   int variant;  // TILE_PASS_LIST or TILE_PASS_RUNS
   int ty, tz;
+  bool plain;
 };
 inline TileCfg decode_tile_cfg(int code, bool d3) {
   TileCfg c;
   const int v = code & 15;
   c.variant = v == TILE_PASS_LIST ? TILE_PASS_LIST : TILE_PASS_RUNS;
   const int shape = (code >> 4) & 15;
+  c.plain = (code & 0x100) != 0;
   if (!d3) { c.ty = 64; c.tz = 1; }
   else if (shape == 1) { c.ty = 4; c.tz = 16; }
   else if (shape == 2) { c.ty = 16; c.tz = 4; }
@@ -38,7 +41,8 @@ inline TileCfg decode_tile_cfg(int code, bool d3) {
 }
 inline bool valid_tile_code(int code) {
   const int v = code & 15;
-  return code == 0 || ((v == TILE_PASS_RUNS || v == TILE_PASS_LIST) && (code >> 4) <= 2);
+  return code == 0 || ((v == TILE_PASS_RUNS || v == TILE_PASS_LIST) && ((code >> 4) & 15) <= 2 &&
+                       (code >> 9) == 0);
 }
 
 #define CC3D_DECLARE_DTYPE_LAUNCHERS(SUF)                                              \

@@ -148,6 +148,7 @@ struct LabelArgs {
   uint64_t delta_bits;
   const unsigned long long* span;
   int budget;                  // iteration limit of every union-find loop (0: the defaults)
+  int no_tma;                  // read tile boxes with plain loads even where TMA could
 };
 
 // Geometry of the volume a tile belongs to, and the tile's place in it.

@@ -149,6 +149,24 @@ __device__ __forceinline__ int warp_row(int w, int j) {
 // runs one per block; the persistent batch kernel (cc3d_batch_persistent.cu)
 // runs many in a row (the block's shared memory is free again once it
 // returns).  `tmap` is used only when use_tma is set.
+// The unions of a warp's pair buffer q[0, n), lane i taking entries i, i + 32,
+// ... (pairs (a << 16) | b).  Not inlined: every site that flushes the buffer
+// shares one copy of the union-find code.  Returns 1 if a union ran out of
+// budget.
+template <typename PT>
+static __device__ __noinline__ int list_unions(const uint32_t* q, int n, PT* par, int lim, int lane) {
+  __syncwarp();
+  int err = 0;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    if (r0 + lane < n) {
+      const uint32_t e = q[r0 + lane];
+      if (!lunite<PT>(par, e >> 16, e & 0xFFFFu, lim)) err = 1;
+    }
+  }
+  __syncwarp();
+  return err;
+}
+
 template <typename T, int CONN, int TY, int TZ, int MODE>
 __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtensorMap* tmap, int use_tma,
                                                int64_t tile) {
@@ -324,6 +342,7 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
     uint32_t F, E;
     const uint32_t S = masks(rb, F, E);
     if ((S >> lane) & 1u) par[ri * 32 + lane] = (PT)(ri * 32 + lane);
+    rootm[ri] = 0u;
     if (MODE == MODE_MULTI && E) {
       epl_acc += __popc(E);
       frb = rb < frb ? rb : frb;
@@ -417,98 +436,82 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   }
   __syncwarp();
 
-  // the warp's list, one entry per lane: its union pairs are found first (the
-  // needy voxels' relation tests), collected, and run in dense rounds of one
-  // union per lane.  Bits of a lane's pair set: j < NB a needy voxel's
-  // relation j; NB the column x0 - 1 of its row; NB + 1 the row-level pair
-  // with the row behind (6); NB + 2 the row-level pair with the link row.
+  // the warp's list, one entry per lane: each lane tests its voxel's
+  // relations one after the other (a needy voxel's own relation tests; the
+  // column x0 - 1 of its row; the row-level pair with the row behind (6); the
+  // row-level pair with the link row), and after each relation the lanes
+  // that hold it append their pair to the warp's pair buffer in one step;
+  // the buffer's unions run in dense rounds of one union per lane.
   int err = 0;
   int pc = 0;  // warp-uniform pair fill
   uint32_t* pw = pairs[warp];
-  auto run_pairs = [&]() {
-    __syncwarp();
-    for (int r0 = 0; r0 < pc; r0 += 32) {
-      if (r0 + lane < pc) {
-        const uint32_t q = pw[r0 + lane];
-        if (!lunite<PT>(par, q >> 16, q & 0xFFFFu, llim)) err = 1;
-      }
-    }
-    __syncwarp();
-    pc = 0;
-  };
   for (int r0 = 0; r0 < un; r0 += 32) {
     const int i = r0 + lane;
-    uint32_t m = 0;
+    unsigned e = 0;
     int x = 0, rb = 0;
-    unsigned short h = 0;
+    uint32_t h = 0;
     if (i < un) {
-      const unsigned e = ul[i];
+      e = ul[i];
       x = (int)(e & 31u);
-      const int ri = (int)((e >> 5) & 63u);
-      const unsigned km = (e >> 11) & 7u;
-      rb = rb_of(ri);
-      const uint32_t Sc = smask[rb];
-      h = (unsigned short)(ri * 32 + head_of(Sc, x));
-      m = ((km & 4u) ? 1u << NB : 0u) | ((km & 1u) ? 2u << NB : 0u) | ((km & 2u) ? 4u << NB : 0u);
-      if (PRIMARY && ((e >> 14) & 1u)) {
-        // a needy voxel tests its remaining relations itself
-        const T v = at(rb, x);
-        const bool head = (Sc >> x) & 1u;
-#pragma unroll
-        for (int j = 0; j < NB; ++j) {
-          const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
-          const int k = (int)(c & 3u), dx = (int)(c >> 2) - 1;
-          const int rbk = rb + row_off(k);
-          bool rel = (head || !((NRel::left >> j) & 1u)) && R(v, at(rbk, x + dx));
-          if (dx != 0) {
-            // the neighbour run of column x + dx already joined through the
-            // dx = 0 relation when it also covers column x
-            const int xn = x + dx;
-            const uint32_t Sk = smask[rbk];
-            const bool same = (xn >= 0 && xn <= 31) && !((Sk >> (dx > 0 ? xn : x)) & 1u);
-            rel = rel && !(same && R(v, at(rbk, x)));
-          }
-          if (rel) m |= 1u << j;
-        }
-        // the column x0 - 1 of the voxel's own row
-        if (x == 0 && R(v, at(rb, -1))) m |= 1u << NB;
-      }
+      rb = rb_of((int)((e >> 5) & 63u));
+      h = (uint32_t)(((e >> 5) & 63u) * 32u + head_of(smask[rb], x));
     }
-    // collect the pairs, one per lane per step
-    while (__any_sync(FULL, m != 0u)) {
-      const uint32_t act = __ballot_sync(FULL, m != 0u);
-      if (pc + __popc(act) > PC) run_pairs();
-      if (m) {
-        const int j = __ffs(m) - 1;
-        m &= m - 1u;
-        int rbk, xn = x;
-        if (j < NB) {
-          const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
-          const int k = (int)(c & 3u);
-          xn = x + (int)(c >> 2) - 1;
-          rbk = rb + (k == 0 ? row_off(0) : (k == 1 ? row_off(1) : (k == 2 ? row_off(2) : row_off(3))));
-        } else {
-          rbk = j == NB ? rb : (j == NB + 1 ? rb - 1 : rb + LOFF);
-          if (j == NB) xn = -1;
-        }
-        unsigned short t;
-        if (xn < 0) t = (unsigned short)(CNODE + rbk);
-        else if (xn > 31) t = (unsigned short)(CNODE + NRB + rbk);
-        else t = (unsigned short)(nbase[rbk] + head_of(smask[rbk], xn));
-        pw[pc + __popc(act & lt)] = ((uint32_t)h << 16) | t;
+    // append pair (h, t) for every lane with `has`
+    auto emit = [&](bool has, uint32_t t) {
+      const uint32_t act = __ballot_sync(FULL, has);
+      if (!act) return;
+      if (pc + __popc(act) > PC) {
+        err |= list_unions<PT>(pw, pc, par, llim, lane);
+        pc = 0;
       }
+      if (has) pw[pc + __popc(act & lt)] = (h << 16) | t;
       pc += __popc(act);
+    };
+    // the target node of column xn of box row rbk
+    auto node_at = [&](int rbk, int xn) -> uint32_t {
+      if (xn < 0) return (uint32_t)(CNODE + rbk);
+      if (xn > 31) return (uint32_t)(CNODE + NRB + rbk);
+      return (uint32_t)(nbase[rbk] + head_of(smask[rbk], xn));
+    };
+    if constexpr (PRIMARY) {
+      // a needy voxel tests its remaining relations itself
+      const bool needy = (e >> 14) & 1u;
+      const T v = at(rb, x);
+      const bool head = (smask[rb] >> x) & 1u;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const unsigned c = (unsigned)((NRel::code >> (4 * j)) & 15u);
+        const int k = (int)(c & 3u), dx = (int)(c >> 2) - 1;
+        const int rbk = rb + row_off(k);
+        bool rel = needy && (head || !((NRel::left >> j) & 1u)) && R(v, at(rbk, x + dx));
+        if (dx != 0) {
+          // the neighbour run of column x + dx already joined through the
+          // dx = 0 relation when it also covers column x
+          const int xn = x + dx;
+          const uint32_t Sk = smask[rbk];
+          const bool same = (xn >= 0 && xn <= 31) && !((Sk >> (dx > 0 ? xn : x)) & 1u);
+          rel = rel && !(same && R(v, at(rbk, x)));
+        }
+        emit(rel, node_at(rbk, x + dx));
+      }
+      // the column x0 - 1 of the voxel's own row
+      emit(needy && x == 0 && R(v, at(rb, -1)), (uint32_t)(CNODE + rb));
+    } else {
+      emit(((e >> 11) & 4u) != 0u, (uint32_t)(CNODE + rb));
+      if constexpr (CONN == 6) emit(((e >> 11) & 1u) != 0u, node_at(rb - 1, x));
     }
+    emit(((e >> 11) & 2u) != 0u, node_at(rb + LOFF, x));
   }
-  run_pairs();
+  err |= list_unions<PT>(pw, pc, par, llim, lane);
   if (err) local_err = 1;
   __syncthreads();
 
-  // ---- phase C: roots, run records, keys, bitmap, warp by warp from the
-  // bottom of its columns up.  A component is named by its root run (the
-  // smallest node of its tree, its first run in raster order): the run's
-  // index in the tile's run order.  Halo heads and the halo columns are only
-  // pointed at their roots, for the edges below.
+  // ---- phase C: roots, run records, keys, bitmap.  A component is named by
+  // its root run (the smallest node of its tree, its first run in raster
+  // order): the run's index in the tile's run order.  Each warp gathers the
+  // run heads of its rows (bottom of its columns first) into its list and
+  // resolves them 32 at a time, one per lane.  Halo heads and the halo
+  // columns are only pointed at their roots, for the edges below.
   const uint32_t C = rbase[NR];
   auto rid_of = [&](unsigned r) -> unsigned {
     return rbase[r >> 5] + __popc(smask[rb_of((int)(r >> 5))] & ((1u << (r & 31u)) - 1u));
@@ -517,14 +520,19 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   const uint32_t sy32 = (uint32_t)g.sy;
   // bitmap word of the tile's row (ly, lz) = bw0 + (lz * sy + ly) * wpr
   const uint32_t bw0 = (uint32_t)g.word0 + ((uint32_t)z0 * sy32 + (uint32_t)y0) * wpr + tx;
+  int nh = 0;  // warp-uniform head count
   for (int j = 0; j < RPW; ++j) {
-    const int ri = warp_row<TY>(warp, j), rb = rb_of(ri);
-    const uint32_t S = smask[rb];
-    bool root = false;
-    uint32_t r = 0;
-    if ((S >> lane) & 1u) {
-      const uint32_t n = (uint32_t)(ri * 32 + lane);
-      r = lfind_ro<PT>(par, n, llim);
+    const int ri = warp_row<TY>(warp, j);
+    const uint32_t S = smask[rb_of(ri)];
+    if ((S >> lane) & 1u) ul[nh + __popc(S & lt)] = (unsigned short)(ri * 32 + lane);
+    nh += __popc(S);
+  }
+  __syncwarp();
+  for (int h0 = 0; h0 < nh; h0 += 32) {
+    if (h0 + lane < nh) {
+      const uint32_t n = ul[h0 + lane];
+      const int ri = (int)(n >> 5), x = (int)(n & 31u);
+      uint32_t r = lfind_ro<PT>(par, n, llim);
       if (par[r] != r) {
         // the find ran out of budget: the run becomes a root of its own (the
         // call reports the error), so every component it names has a key
@@ -532,15 +540,15 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
         r = n;
       }
       par[n] = (PT)r;
-      root = r == n;
       const unsigned c = rid_of(r);
-      p.rcomp[node0 + rbase[ri] + __popc(S & lt)] = (uint16_t)c;
-      if (root) {
+      const unsigned own = rbase[ri] + __popc(smask[rb_of(ri)] & ((1u << x) - 1u));
+      p.rcomp[node0 + own] = (uint16_t)c;
+      if (r == n) {
         const uint32_t bw = bw0 + ((uint32_t)(ri / TY) * sy32 + (uint32_t)(ri % TY)) * wpr;
-        p.E[node0 + c] = ((unsigned long long)(bw * 32u + (uint32_t)lane) << 32) | (node0 + c);
+        p.E[node0 + c] = ((unsigned long long)(bw * 32u + (uint32_t)x) << 32) | (node0 + c);
+        atomicOr(&rootm[ri], 1u << x);
       }
     }
-    rootm[ri] = __ballot_sync(FULL, root);
   }
   for (int h = warp; h < NHR; h += NW) {
     const uint32_t S = smask[halo_rb(h)];

@@ -335,7 +335,8 @@ int cc3d_gpu_stack_relabel(const void* labels, int label_bytes, const int64_t* l
  * Tile-pass configurations and their autotuner.  No counterpart in the
  * reference, which has a single CPU algorithm per connectivity.  Every
  * configuration gives identical labels; they differ only in speed.
- * A configuration code is a variant ORed with a 3D tile shape:
+ * A configuration code is a variant ORed with a 3D tile shape and a load
+ * path:
  *   CC3D_TILE_LIST  one 256-thread block per tile: each row is related to
  *                   its primary neighbour row by one ballot; voxels that
  *                   relation does not decide go to per-warp lists and are
@@ -348,18 +349,21 @@ int cc3d_gpu_stack_relabel(const void* labels, int label_bytes, const int64_t* l
  *                   relation mode).
  *   CC3D_TILE_8x8 / _4x16 / _16x4   3D tiles of 32 x 8 x 8, 32 x 4 x 16 or
  *                   32 x 16 x 4 voxels (x y z).  2D images always use 32 x 64.
+ *   CC3D_TILE_PLAIN the tile's box is read by the block's threads with plain
+ *                   loads; without it, by one TMA copy where the volume
+ *                   allows it (16-byte aligned base and rows).  Batches
+ *                   always use plain loads.
  * Binary 8-connected images always use CC3D_TILE_RUNS (2x2-block numbering).
  *
  * cc3d_gpu_set_tile_pass: the calling thread's configuration (CC3D_TILE_AUTO
- *   = the autotuned choice for the volume's class, else LIST | 16x4 for
- *   volumes of 2^24 voxels or more at 18/26-connectivity and LIST | 8x8
- *   otherwise); returns
+ *   = the autotuned choice for the volume's class, else LIST | 8x8); returns
  *   the previous setting, or CC3D_ERR_INVALID for an unknown code.
  * cc3d_gpu_tile_pass_choice: the configuration a labelling of this volume
  *   would use now.
- * cc3d_gpu_tile_config: code of configuration `index` in 0..CC3D_TILE_CONFIGS-1
- *   (LIST|8x8, RUNS|8x8, LIST|4x16, RUNS|4x16, LIST|16x4, RUNS|16x4).
- * cc3d_gpu_autotune: times every configuration on `in` (2D: the first two;
+ * cc3d_gpu_tile_config: code of configuration `index` in 0..CC3D_TILE_CONFIGS-1:
+ *   for each shape (8x8, 4x16, 16x4), for each variant (LIST, RUNS), the
+ *   TMA box then the plain-load box: 12 configurations.
+ * cc3d_gpu_autotune: times every configuration on `in` (2D: the first four;
  *   best of `repeats` after one warm-up run each), records the fastest for
  *   the volume's class (dtype, effective connectivity, binary or not, voxel
  *   count within a factor of 8) and returns it in *best; ms[index] gets each
@@ -373,7 +377,8 @@ int cc3d_gpu_stack_relabel(const void* labels, int label_bytes, const int64_t* l
 #define CC3D_TILE_8x8 0x00
 #define CC3D_TILE_4x16 0x10
 #define CC3D_TILE_16x4 0x20
-#define CC3D_TILE_CONFIGS 6
+#define CC3D_TILE_PLAIN 0x100
+#define CC3D_TILE_CONFIGS 12
 #define CC3D_TILE_MODEL 3   /* policy: the cost model's choice per volume (below) */
 int cc3d_gpu_set_tile_pass(int code);
 int cc3d_gpu_tile_pass_choice(int dtype, int64_t sx, int64_t sy, int64_t sz,
@@ -412,7 +417,7 @@ void cc3d_gpu_autotune_reset(void);
  * otherwise they behave as CC3D_TILE_AUTO.
  */
 #define CC3D_COST_FEATURES 16
-#define CC3D_COST_PARAMS 5682
+#define CC3D_COST_PARAMS 6084
 int cc3d_gpu_volume_features(const void* in, int dtype, int64_t sx, int64_t sy, int64_t sz,
                              int64_t connectivity, int binary_image, int mem_flags, void* stream,
                              float* features);

@@ -41,18 +41,18 @@ def test_train_predict_choose(cc3d):
     import torch
     cm = cc3d.costmodel
     X, Y, desc = cm.collect(24, seed=3, lo=24, hi=72)
-    assert X.shape == (24, 16) and Y.shape == (24, 6)
+    assert X.shape == (24, 16) and Y.shape == (24, 12)
     assert np.isfinite(Y).sum() >= 24 * 2
     loss = cm.train(X, Y, epochs=60, batch=8, lr=3e-3, seed=1)
     assert np.isfinite(loss)
     P = cm.predict(X)
-    assert P.shape == (24, 6) and np.all(np.isfinite(P))
+    assert P.shape == (24, 12) and np.all(np.isfinite(P))
     # fitting the training set beats predicting the mean
     m = np.isfinite(Y)
     mean = np.nanmean(Y, axis=0)
     assert ((P - Y)[m] ** 2).mean() < ((mean - Y)[m] ** 2).mean()
     p = cm.get_params()
-    assert p.shape == (5682,)
+    assert p.shape == (6084,)
     cm.set_params(p)
     assert np.array_equal(cm.predict(X), P)
     r = cm.regret(Y, P)

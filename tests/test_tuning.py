@@ -28,12 +28,15 @@ def test_choice_follows_the_thread_setting(cc3d):
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=4) == "runs/8x8"
     cc3d.set_tile_pass("auto")
     cc3d.autotune_reset()
-    # the defaults without tuning data: 32x16x4 tiles for large 18/26-connected volumes
+    # the default without tuning data: the list pass on 32x8x8 tiles, box by TMA
     assert cc3d.tile_pass_choice(vol) == "list/8x8"
     big = np.zeros((256, 256, 256), np.uint8)
-    assert cc3d.tile_pass_choice(big) == "list/16x4"
-    assert cc3d.tile_pass_choice(big, connectivity=18) == "list/16x4"
+    assert cc3d.tile_pass_choice(big) == "list/8x8"
     assert cc3d.tile_pass_choice(big, connectivity=6) == "list/8x8"
+    # the load-path bit survives for 2D images, the shape does not
+    cc3d.set_tile_pass("list/16x4/plain")
+    assert cc3d.tile_pass_choice(vol) == "list/16x4/plain"
+    assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint32), connectivity=8) == "list/8x8/plain"
     # binary 8-connected images always take the run-union pass (2x2-block numbering)
     cc3d.set_tile_pass("list")
     assert cc3d.tile_pass_choice(np.zeros((64, 64), np.uint8), connectivity=8, binary_image=True) == "runs/8x8"
@@ -48,6 +51,9 @@ def test_unknown_variant_is_rejected(cc3d):
     lib = cc3d._native.load()
     assert lib.cc3d_gpu_set_tile_pass(7) == -1
     assert lib.cc3d_gpu_set_tile_pass(0x31) == -1
+    assert lib.cc3d_gpu_set_tile_pass(0x202) == -1
+    with pytest.raises(KeyError):
+        cc3d.set_tile_pass("list/8x8/tma")
     with pytest.raises(KeyError):
         cc3d.set_tile_pass("fastest")
 
@@ -76,4 +82,4 @@ def test_autotune_records_the_fastest_configuration(cc3d):
         cc3d.set_tile_pass("auto")
     img = synth.bernoulli_volume((300, 400), 0.5, seed=3)
     res = cc3d.autotune(img, connectivity=4)
-    assert set(res["ms"]) == {"list/8x8", "runs/8x8"}
+    assert set(res["ms"]) == {"list/8x8", "list/8x8/plain", "runs/8x8", "runs/8x8/plain"}
