@@ -77,7 +77,10 @@ def load(path: str = DEFAULT_PARAMS) -> bool:
     """Load parameters (the ones shipped with the package by default); False if absent."""
     if not os.path.exists(path):
         return False
-    set_params(np.load(path))
+    p = np.load(path)
+    if p.size != N_PARAMS:  # parameters of another model shape
+        return False
+    set_params(p)
     return True
 
 

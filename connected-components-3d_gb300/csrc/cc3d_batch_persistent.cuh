@@ -8,7 +8,7 @@
 //
 //   0  tile -> volume map         one block per volume
 //   1  tile pass                  one block per tile (tile_list_tile)
-//   2  edge merges                one warp per tile (merge_tile_edges)
+//   2  edge merges                one warp per 32 tiles (merge_group_edges)
 //   3  chunk popcounts            one block per bitmap chunk
 //   4  scan of the chunk sums     block 0
 //   5  word prefixes              one block per bitmap chunk
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHead
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_list_tile<T, CONN, TY, TZ, MODE_MULTI>(p, nullptr, 0, t);
   if (!grid_barrier(hdr)) return;
   // 2: edge merges
-  for (int64_t t = gw; t < ntiles; t += nwarps) merge_tile_edges(p, t, lane);
+  for (int64_t g = gw; g * 32 < ntiles; g += nwarps) merge_group_edges(p, g * 32, lane);
   if (!grid_barrier(hdr)) return;
   // 3-5: numbering scan
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)

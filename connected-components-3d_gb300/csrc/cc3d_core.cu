@@ -19,13 +19,12 @@ void* tensor_map_encoder() {
 }
 
 // ------------------------------------------------------- K2: edge merges
-// one warp per tile walks the tile's edge slots (merge_tile_edges)
+// one warp per 32 tiles takes their edges 32 at a time (merge_group_edges)
 __global__ void __launch_bounds__(256) k_merge_edges(LabelArgs p) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < p.ntiles;
-       tile += warps)
-    merge_tile_edges(p, tile, lane);
+  for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g * 32 < p.ntiles; g += warps)
+    merge_group_edges(p, g * 32, lane);
 }
 
 cudaError_t launch_merge_edges(const LabelArgs& a, cudaStream_t s) {

@@ -574,7 +574,7 @@ k_write(LabelArgs p, OUT* out) {
 // have their dependent loads in flight at once.
 constexpr int kLabelWarps = 4;
 template <typename OUT, int TY, int TZ>
-__global__ void __launch_bounds__(kLabelWarps * 32)
+__global__ void __launch_bounds__(kLabelWarps * 32, 12)
 k_label_write(LabelArgs p, OUT* out, int64_t count) {
   __shared__ uint32_t slab[kLabelWarps][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

@@ -26,6 +26,45 @@ __device__ __forceinline__ void merge_tile_edges(const LabelArgs& p, int64_t til
   }
 }
 
+// K2 of the 32 tiles [t0, t0 + 32), by one warp: their edges are numbered one
+// after the other (a warp scan of the tiles' edge counts) and taken 32 at a
+// time, one per lane, so every round of dependent loads serves 32 edges
+// (a tile has a few dozen edges; one warp per tile leaves most lanes of its
+// last round idle).
+__device__ __forceinline__ void merge_group_edges(const LabelArgs& p, int64_t t0, int lane) {
+  const int64_t tile = t0 + lane;
+  const uint32_t n = tile < p.ntiles ? p.tinfo[tile].nedges : 0u;
+  uint32_t incl = n;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t excl = incl - n;
+  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t e = base + lane;
+    // the lane (tile) whose edge range holds e: the last lane with excl <= e
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const uint32_t ex = __shfl_sync(FULL, excl, lo + step);
+      if (ex <= e) lo += step;
+    }
+    const uint32_t slot = e - __shfl_sync(FULL, excl, lo);
+    if (e >= total) continue;
+    const int64_t t = t0 + lo;
+    const uint2 ed = p.edges[t * p.edge_slots + slot];
+    const uint32_t otile = ed.y / kTV, local = ed.y % kTV;
+    if (ed.x >= (uint64_t)p.ntiles * kTV) {
+      atomicOr(&p.ctr->err, ERR_INDEX);
+      continue;
+    }
+    gunite(p.E, ed.x, record_node(p, otile, (int)(local >> 5), (int)(local & 31)), node_count(p), p.bitmap,
+           p.nwords, p.ctr, p.budget);
+  }
+}
+
 // ------------------------------------------------------------ numbering scan
 // The bitmap of surviving component keys is cut into chunks of kScanChunk
 // words; chunk b's popcount goes to bsum[b], then an exclusive scan of the

@@ -211,9 +211,16 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   // 255: none)
   __shared__ uint32_t rtile[NRB];
   __shared__ unsigned char rloc[NRB], rprev[NRB];
-  // per warp: one entry per voxel of its rows that has unions to run:
-  // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x
+  // the tile's list: one entry per voxel that has unions to run,
+  // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x; in phase C
+  // each warp's slice holds the run heads of its rows
   __shared__ unsigned short ulist[NW][QN];
+  // per tile row: the ballot of its relations with its link row (M) and, for
+  // 18 and 6, with the row behind; for 6 and 4 whether x = 0 relates to the
+  // column x0 - 1
+  __shared__ uint32_t mmask[NR], m2mask[NR];
+  __shared__ unsigned char colb[NR];
+  __shared__ unsigned int list_fill;
   // per warp: union pairs (h << 16) | t waiting for a dense round
   constexpr int PC = 64;
   __shared__ uint32_t pairs[NW][PC];
@@ -257,6 +264,7 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   if (tid == 0) {
     local_err = 0;
     edge_fill = 0;
+    list_fill = 0;
     if (use_tma) {
       mbar_init(&tbar, 1);
       fence_mbar_init();
@@ -343,6 +351,12 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
     const uint32_t S = masks(rb, F, E);
     if ((S >> lane) & 1u) par[ri * 32 + lane] = (PT)(ri * 32 + lane);
     rootm[ri] = 0u;
+    // relations with the link row (dx = 0) and, for 18 and 6, the row behind
+    const T v = at(rb, lane);
+    const bool fg = (F >> lane) & 1u;
+    mmask[ri] = __ballot_sync(FULL, fg && R(v, at(rb + LOFF, lane)));
+    if constexpr (CONN == 18 || CONN == 6) m2mask[ri] = __ballot_sync(FULL, fg && R(v, at(rb - 1, lane)));
+    if constexpr (CONN == 6 || CONN == 4) colb[ri] = (unsigned char)((F & 1u) && R(at(rb, 0), at(rb, -1)));
     if (MODE == MODE_MULTI && E) {
       epl_acc += __popc(E);
       frb = rb < frb ? rb : frb;
@@ -357,14 +371,82 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   }
   __syncthreads();
 
-  // ---- phase B: row-level relations and unions, warp by warp.  The first
-  // pair of every run with its link row becomes a direct parent link (to a
-  // smaller node, so roots stay the smallest node of their tree; by CAS, as
-  // other warps' unions may already have linked the run); where the link row
-  // is a halo row, each halo run's first pair links the halo run under the
-  // tile run instead.  The other row-level pairs and the needy voxels go to
-  // the warp's list, whose unions run once its rows are done.
-  if (warp == 0) {
+  // ---- phase B1: row-level relations, one lane per tile row (warps 0 and
+  // 1), on the row masks.  The first pair of every run with its link row
+  // becomes a direct parent link (to the link row's run's parent at that
+  // moment: a smaller node, so roots stay the smallest node of their tree);
+  // where the link row is a halo row, each halo run's first pair links the
+  // halo run under the tile run instead.  The other row-level pairs and the
+  // needy voxels go to the tile's list, whose unions run in phase B2 (no
+  // union runs before every direct link is in place).
+  if (warp < 2) {
+    const int ri = warp * 32 + lane, rb = rb_of(ri), rl = rb + LOFF;
+    const uint32_t F = fmask[rb], Sc = smask[rb], Sl = smask[rl], M = mmask[ri];
+    const uint32_t P = M & (Sc | Sl | ~(M << 1));
+    uint32_t NEED = 0, K1 = 0, K4 = 0, K2 = 0;
+    if constexpr (CONN == 26 || CONN == 8) {
+      // a needy voxel that continues a run whose next voxel relates to its
+      // primary neighbour needs nothing: it only has dx = +1 relations of its
+      // own, and each of them is that next voxel's dx = 0 relation, implied
+      NEED = F & ~M & ~(~Sc & (M >> 1) & ~(Sc >> 1) & 0x7FFFFFFFu);
+    } else if constexpr (CONN == 18) {
+      NEED = F & ~(M & m2mask[ri]);
+    } else {
+      // 6: every starting pair of runs with the row behind; 6 and 4: x = 0
+      // with the column x0 - 1
+      if constexpr (CONN == 6) {
+        const uint32_t M0 = m2mask[ri];
+        K1 = M0 & (Sc | smask[rb - 1] | ~(M0 << 1));
+      }
+      K4 = colb[ri] ? 1u : 0u;
+    }
+    // walk the pair starts in x order: a run's (halo run's) first pair is the
+    // first pair start seen under its head
+    uint32_t rest = P;
+    int last = -1;
+    while (rest) {
+      const int x = __ffs(rest) - 1;
+      rest &= rest - 1u;
+      if (ri >= LROW0) {
+        const int hx = head_of(Sc, x);
+        if (hx != last) {
+          last = hx;
+          const uint32_t tl = (uint32_t)((ri - LSTEP) * 32 + head_of(Sl, x));
+          par[ri * 32 + hx] = ((const volatile PT*)par)[tl];
+        } else {
+          K2 |= 1u << x;
+        }
+      } else {
+        const int hl = head_of(Sl, x);
+        if (hl != last) {
+          last = hl;
+          par[nbase[rl] + hl] = (PT)(ri * 32 + head_of(Sc, x));
+        } else {
+          K2 |= 1u << x;
+        }
+      }
+    }
+    // this row's list entries, placed after the earlier lanes' of the warp
+    const uint32_t U = NEED | K1 | K2 | K4;
+    const unsigned cnt = __popc(U);
+    unsigned incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    unsigned base = 0;
+    if (lane == 31) base = atomicAdd(&list_fill, incl);
+    base = __shfl_sync(FULL, base, 31) + incl - cnt;
+    unsigned short* tl_ = &ulist[0][0];
+    uint32_t u = U;
+    while (u) {
+      const int x = __ffs(u) - 1;
+      u &= u - 1u;
+      const unsigned km = ((K1 >> x) & 1u) | (((K2 >> x) & 1u) << 1) | (((K4 >> x) & 1u) << 2);
+      tl_[base++] = (unsigned short)((((NEED >> x) & 1u) << 14) | (km << 11) | ((unsigned)ri << 5) | (unsigned)x);
+    }
+  } else if (warp == 2) {
     // exclusive prefix of the run counts over the tile rows (two per lane)
     const uint32_t a0 = __popc(smask[rb_of(2 * lane)]), a1 = __popc(smask[rb_of(2 * lane + 1)]);
     uint32_t sa = a0 + a1;
@@ -377,65 +459,12 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
     rbase[2 * lane + 1] = (unsigned short)(sa - a1);
     if (lane == 31) rbase[NR] = (unsigned short)sa;
   }
-  int un = 0;  // warp-uniform list fill
-  unsigned short* ul = ulist[warp];
-  for (int j = 0; j < RPW; ++j) {
-    const int ri = warp_row<TY>(warp, j), rb = rb_of(ri);
-    const int rl = rb + LOFF;
-    const T v = at(rb, lane);
-    const uint32_t F = fmask[rb], Sc = smask[rb], Sl = smask[rl];
-    const bool fg = (F >> lane) & 1u;
-    const uint32_t M = __ballot_sync(FULL, fg && R(v, at(rl, lane)));
-    const uint32_t P = M & (Sc | Sl | ~(M << 1));
-    uint32_t NEED = 0, km = 0;
-    if constexpr (CONN == 26 || CONN == 8) {
-      // a needy voxel that continues a run whose next voxel relates to its
-      // primary neighbour needs nothing: it only has dx = +1 relations of its
-      // own, and each of them is that next voxel's dx = 0 relation, implied
-      NEED = F & ~M & ~(~Sc & (M >> 1) & ~(Sc >> 1) & 0x7FFFFFFFu);
-    } else if constexpr (CONN == 18) {
-      NEED = F & ~(M & __ballot_sync(FULL, fg && R(v, at(rb - 1, lane))));
-    } else {
-      // 6: the row behind too; 6 and 4: lane 0 and the column x0 - 1
-      if constexpr (CONN == 6) {
-        const uint32_t M0 = __ballot_sync(FULL, fg && R(v, at(rb - 1, lane)));
-        km = ((M0 & (Sc | smask[rb - 1] | ~(M0 << 1))) >> lane) & 1u;
-      }
-      if (lane == 0 && fg && R(v, at(rb, -1))) km |= 4u;
-    }
-    if ((P >> lane) & 1u) {
-      const int hx = head_of(Sc, lane);
-      const uint32_t h = (uint32_t)(ri * 32 + hx);
-      if (ri >= LROW0) {
-        // this run's first pair: parent = the link row's run
-        if ((P & lt & ~((1u << hx) - 1u)) == 0u) {
-          // the link row's run, or already its parent: the link row is
-          // normally one of this warp's earlier rows, whose runs point down
-          // their column, so every run of a column points at its bottom run
-          const uint32_t tl = (uint32_t)((ri - LSTEP) * 32 + head_of(Sl, lane));
-          const uint32_t t = ((const volatile PT*)par)[tl];
-          if ((uint32_t)atomicCAS(&par[h], (PT)h, (PT)t) != h) km |= 2u;
-        } else {
-          km |= 2u;
-        }
-      } else {
-        // the halo run's first pair: the halo run's parent = this run
-        const int hl = head_of(Sl, lane);
-        if ((P & lt & ~((1u << hl) - 1u)) == 0u) {
-          const uint32_t hn = (uint32_t)(nbase[rl] + hl);
-          if ((uint32_t)atomicCAS(&par[hn], (PT)hn, (PT)h) != hn) km |= 2u;
-        } else {
-          km |= 2u;
-        }
-      }
-    }
-    const unsigned need = (NEED >> lane) & 1u;
-    const uint32_t Q = __ballot_sync(FULL, (km | need) != 0u);
-    if ((Q >> lane) & 1u) ul[un + __popc(Q & lt)] = (unsigned short)((need << 14) | (km << 11) | (ri << 5) | lane);
-    un += __popc(Q);
-  }
-  __syncwarp();
+  __syncthreads();
 
+  // ---- phase B2: the tile's list, 32 entries per warp and round
+  const int un = (int)list_fill;
+  const unsigned short* tlist = &ulist[0][0];
+  unsigned short* ul = ulist[warp];
   // the warp's list, one entry per lane: each lane tests its voxel's
   // relations one after the other (a needy voxel's own relation tests; the
   // column x0 - 1 of its row; the row-level pair with the row behind (6); the
@@ -445,13 +474,13 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   int err = 0;
   int pc = 0;  // warp-uniform pair fill
   uint32_t* pw = pairs[warp];
-  for (int r0 = 0; r0 < un; r0 += 32) {
+  for (int r0 = warp * 32; r0 < un; r0 += NW * 32) {
     const int i = r0 + lane;
     unsigned e = 0;
     int x = 0, rb = 0;
     uint32_t h = 0;
     if (i < un) {
-      e = ul[i];
+      e = tlist[i];
       x = (int)(e & 31u);
       rb = rb_of((int)((e >> 5) & 63u));
       h = (uint32_t)(((e >> 5) & 63u) * 32u + head_of(smask[rb], x));
@@ -590,27 +619,34 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   // in one component of their own tile, so that edge would repeat
   uint2* edges = p.edges + (size_t)utile * p.edge_slots;
   constexpr int NCC = (2 * NRB + 31) / 32;  // 32-voxel chunks of the two halo columns
-  for (int it = warp; it < NHR + NCC; it += NW) {
-    bool has = false;
-    uint2 e = make_uint2(0u, 0u);
-    if (it < NHR) {
-      const int rb = halo_rb(it);
-      if ((smask[rb] >> lane) & 1u) {  // run heads stand for their runs
-        const uint32_t r = par[HNODE + it * 32 + lane];
-        if (r < kTV) {
-          has = true;
-          const int rp = rprev[rb];
-          if (rp != 255) {
-            const T a = at(rb, lane), b = at(rp, lane);
-            if (b != T(0) && (MODE == MODE_MULTI ? a == b : true) &&
-                par[nbase[rp] + head_of(smask[rp], lane)] == r)
-              has = false;
-          }
-          if (has) e = make_uint2(node0 + rid_of(r), (rtile[rb] * (uint32_t)kRowsPerTile + rloc[rb]) * 32u + lane);
+  constexpr int NHW = (NHR + 31) / 32;      // warps that take the halo rows, one lane per row
+  static_assert(NHW + 1 <= NW, "warps left for the halo columns");
+  if (warp < NHW) {
+    // halo row h: its run heads in x order
+    const int h = warp * 32 + lane;
+    if (h < NHR) {
+      const int rb = halo_rb(h), rp = rprev[rb];
+      uint32_t heads = smask[rb];
+      const uint32_t Sp = rp != 255 ? smask[rp] : 0u;
+      while (heads) {
+        const int x = __ffs(heads) - 1;
+        heads &= heads - 1u;
+        const uint32_t r = par[HNODE + h * 32 + x];
+        if (r >= kTV) continue;
+        if (rp != 255) {
+          const T a = at(rb, x), b = at(rp, x);
+          if (b != T(0) && (MODE == MODE_MULTI ? a == b : true) && par[nbase[rp] + head_of(Sp, x)] == r) continue;
         }
+        const unsigned slot = atomicAdd(&edge_fill, 1u);
+        if (slot < p.edge_slots)
+          edges[slot] = make_uint2(node0 + rid_of(r), (rtile[rb] * (uint32_t)kRowsPerTile + rloc[rb]) * 32u + x);
       }
-    } else {
-      const int c = (it - NHR) * 32 + lane;
+    }
+  } else {
+    for (int it = warp - NHW; it < NCC; it += NW - NHW) {
+      bool has = false;
+      uint2 e = make_uint2(0u, 0u);
+      const int c = it * 32 + lane;
       if (c < 2 * NRB) {
         const int side = c >= NRB ? 1 : 0, rb = c - side * NRB, xi = side ? 32 : -1;
         if (at(rb, xi) != T(0)) {
@@ -632,15 +668,15 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
           }
         }
       }
-    }
-    const unsigned m = __ballot_sync(FULL, has);
-    if (!m) continue;
-    unsigned base = 0;
-    if (lane == 0) base = atomicAdd(&edge_fill, (unsigned)__popc(m));
-    base = __shfl_sync(FULL, base, 0);
-    if (has) {
-      const unsigned slot = base + __popc(m & lt);
-      if (slot < p.edge_slots) edges[slot] = e;
+      const unsigned m = __ballot_sync(FULL, has);
+      if (!m) continue;
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(&edge_fill, (unsigned)__popc(m));
+      base = __shfl_sync(FULL, base, 0);
+      if (has) {
+        const unsigned slot = base + __popc(m & lt);
+        if (slot < p.edge_slots) edges[slot] = e;
+      }
     }
   }
 

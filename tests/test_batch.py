@@ -91,7 +91,9 @@ def test_autotune_batch_records_a_choice(cc3d):
     vols = _voronoi_batch(_shapes(rng, 16, 16, 64), seed=5)
     from cc3d_gb300.tuning import CONFIGS
     res = cc3d.autotune_batch(vols, connectivity=26)
-    assert res["best"] in CONFIGS and set(res["ms"]) == set(CONFIGS)
+    # (batches read their boxes with plain loads: the load-path variants are not timed)
+    timed = {c for c in CONFIGS if not c.endswith("/plain")}
+    assert res["best"] in timed and set(res["ms"]) == timed
     assert all(v > 0 for v in res["ms"].values())
     _check_batch(cc3d, vols, 26, n_oracle=1)
 
