@@ -819,7 +819,7 @@ def measure_batch(vols, steps: int, warmup: int) -> dict:
         w = 2 if code == nat.U16 else 4
         out_bytes += w * d.numel()
         got = pool[offs[i]:offs[i] + w * d.numel()]
-        ref = o.view(torch.uint8)[:w * d.numel()]  # (a uint16 result fills the buffer's first half)
+        ref = o.reshape(-1).view(torch.uint8)[:w * d.numel()]  # (a uint16 result fills the first half)
         mismatches += int(pn != N or code != pcode or not torch.equal(got, ref))
     peak, peak_kind = load_peaks()
     alg_bytes = voxels * 2 + out_bytes

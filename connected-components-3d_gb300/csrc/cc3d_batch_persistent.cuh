@@ -8,12 +8,13 @@
 //
 //   0  tile -> volume map         one block per volume
 //   1  tile pass                  one block per tile (tile_list_tile)
-//   2  edge merges                one warp per 32 tiles (merge_group_edges)
+//   2  edge merges                one warp per 4 tiles (merge_group_edges)
 //   3  chunk popcounts            one block per bitmap chunk
 //   4  scan of the chunk sums     block 0
 //   5  word prefixes              one block per bitmap chunk
 //   6  per-volume results         one warp per volume (finalize_volume)
-//   7  labels                     one warp per tile (write_batch_tile)
+//   7  run labels                 one warp per tile (resolve_tile)
+//   8  labels                     one block per tile (write_tile)
 //
 // Every argument -- the buffers, the tile and word counts, the volume
 // descriptors -- comes from a header in device memory uploaded before the
@@ -74,67 +75,6 @@ __device__ __forceinline__ bool grid_barrier(PersistentHeader* h) {
   return s_ok != 0;
 }
 
-// Labels of one tile of a batch, by one warp: the labels of the tile's root
-// runs (1 + rank of their root's key within the volume's key range), every
-// other run's label (its root run's), then the tile's 64 rows in the
-// volume's output type.  Run labels go through the per-run global slots.
-template <int TY, int TZ>
-__device__ __forceinline__ void write_batch_tile(const LabelArgs& p, int64_t tile, int lane) {
-  const VolGeo& v = p.vols[p.tile_vol[tile]];
-  const TileGeo g = tile_geo(p, tile);
-  uint32_t C = p.tinfo[tile].C;
-  if (C > kTV) {
-    if (lane == 0) atomicOr(&p.ctr->err, ERR_INDEX);
-    C = kTV;
-  }
-  const uint32_t node0 = (uint32_t)(tile * kTV);
-  const uint32_t rank0 = (uint32_t)v.rank0;
-  uint32_t* lab = p.label + node0;
-  const uint2 ma = p.rmask[tile * kRowsPerTile + lane], mb = p.rmask[tile * kRowsPerTile + 32 + lane];
-  const uint32_t ra = p.rrow[tile * kRowsPerTile + lane], rb = p.rrow[tile * kRowsPerTile + 32 + lane];
-  for (uint32_t c = lane; c < C; c += 32) {
-    if (p.rcomp[node0 + c] != c) continue;  // only root runs name components
-    const uint32_t R = gfind(p.E, node0 + c, node_count(p), p.ctr, limit_of(p.budget, kFindLimit));
-    uint32_t l = 0;
-    if (R != kBadNode) {
-      const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
-      const uint32_t w = key >> 5;
-      if (w < p.nwords) l = p.prefix[w] + __popc(p.bitmap[w] & ((1u << (key & 31)) - 1u)) + 1u - rank0;
-      else atomicOr(&p.ctr->err, ERR_INDEX);
-    }
-    lab[c] = l;
-  }
-  __syncwarp();
-  for (uint32_t c = lane; c < C; c += 32) {
-    const uint32_t rc = p.rcomp[node0 + c];
-    if (rc == c) continue;
-    if (rc < C) lab[c] = lab[rc];
-    else atomicOr(&p.ctr->err, ERR_INDEX);
-  }
-  __syncwarp();
-  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
-  const int64_t x = x0 + lane;
-  const bool xin = x < g.sx;
-  for (int ri = 0; ri < kRowsPerTile; ++ri) {
-    const uint32_t F = __shfl_sync(FULL, ri < 32 ? ma.x : mb.x, ri & 31);
-    const uint32_t S = __shfl_sync(FULL, ri < 32 ? ma.y : mb.y, ri & 31);
-    const uint32_t b = __shfl_sync(FULL, ri < 32 ? ra : rb, ri & 31);
-    const int ly = ri % TY, lz = ri / TY;
-    const int64_t y = y0 + ly, z = z0 + lz;
-    if (!xin || y >= g.sy || z >= g.sz) continue;
-    uint32_t l = 0;
-    if ((F >> lane) & 1u) {
-      const int k = __popc(S & lanemask_le(lane)) - 1;
-      const uint32_t r = b + (uint32_t)k;
-      if (k >= 0 && r < C) l = lab[r];
-      else atomicOr(&p.ctr->err, ERR_INDEX);
-    }
-    const int64_t i = (z * g.sy + y) * g.sx + x;
-    if (v.out_code == 2) static_cast<uint16_t*>(v.out)[i] = (uint16_t)l;
-    else static_cast<uint32_t*>(v.out)[i] = l;
-  }
-}
-
 template <typename T, int CONN>
 __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHeader* hdr) {
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
@@ -161,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHead
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_list_tile<T, CONN, TY, TZ, MODE_MULTI>(p, nullptr, 0, t);
   if (!grid_barrier(hdr)) return;
   // 2: edge merges
-  for (int64_t g = gw; g * 32 < ntiles; g += nwarps) merge_group_edges(p, g * 32, lane);
+  for (int64_t g = gw; g * kMergeGroup < ntiles; g += nwarps) merge_group_edges<kMergeGroup>(p, g * kMergeGroup, lane);
   if (!grid_barrier(hdr)) return;
   // 3-5: numbering scan
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
@@ -174,8 +114,16 @@ __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHead
   // 6: per-volume results
   for (int64_t v = gw; v < nv; v += nwarps) finalize_volume(p, (int)v, nv, nwords, hdr->res, lane);
   if (!grid_barrier(hdr)) return;
-  // 7: labels
-  for (int64_t t = gw; t < ntiles; t += nwarps) write_batch_tile<TY, TZ>(p, t, lane);
+  // 7: run labels, one warp per tile
+  for (int64_t t = gw; t < ntiles; t += nwarps) resolve_tile(p, t, lane);
+  if (!grid_barrier(hdr)) return;
+  // 8: the labels written, one block per tile (write_tile), in the volume's
+  // output type
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const VolGeo& v = p.vols[p.tile_vol[t]];
+    if (v.out_code == 2) write_tile<uint16_t, TY, TZ>(p, t, static_cast<uint16_t*>(v.out));
+    else write_tile<uint32_t, TY, TZ>(p, t, static_cast<uint32_t*>(v.out));
+  }
 }
 
 // the kernel of a dtype and connectivity (null if not built)

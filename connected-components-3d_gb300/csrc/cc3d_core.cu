@@ -19,16 +19,22 @@ void* tensor_map_encoder() {
 }
 
 // ------------------------------------------------------- K2: edge merges
-// one warp per 32 tiles takes their edges 32 at a time (merge_group_edges)
+// one warp per kMergeGroup tiles takes their edges 32 at a time (merge_group_edges)
 __global__ void __launch_bounds__(256) k_merge_edges(LabelArgs p) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g * 32 < p.ntiles; g += warps)
-    merge_group_edges(p, g * 32, lane);
+  for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g * kMergeGroup < p.ntiles;
+       g += warps)
+    merge_group_edges<kMergeGroup>(p, g * kMergeGroup, lane);
 }
 
 cudaError_t launch_merge_edges(const LabelArgs& a, cudaStream_t s) {
-  k_merge_edges<<<152 * 8, 256, 0, s>>>(a);
+  // a warp per group of tiles, up to 32 warps per SM
+  const int64_t groups = (a.ntiles + kMergeGroup - 1) / kMergeGroup;
+  int64_t blocks = (groups + 7) / 8;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_merge_edges<<<(unsigned)blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -60,72 +66,11 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
 }
 
 // ---------------------------------------------------------------- resolve
-// Final label of every run: 1 + rank of the key of its component's root
-// among the surviving keys.  A tile's components are named by their root runs
-// (the runs whose component id is their own index): the labels of the root
-// runs are resolved first, then every other run copies its root run's label
-// into its own slot (slots of non-root runs are never read as component
-// labels, so the copy is safe in place).  One warp per tile; each lane takes
-// 8 runs at a time with all their loads in flight together.
+// one warp per tile (resolve_tile)
 __global__ void __launch_bounds__(256) k_resolve(LabelArgs p, int64_t ntiles) {
-  const int lane = threadIdx.x & 31;
   const int64_t tile = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   if (tile >= ntiles) return;
-  uint32_t C = p.tinfo[tile].C;
-  if (C > kTV) C = kTV;
-  const uint32_t node0 = (uint32_t)(tile * kTV);
-  // a batch numbers each volume from 1: subtract the keys of the volumes before it
-  const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
-  constexpr int PER = 8;
-  for (uint32_t base = 0; base < C; base += 32 * PER) {
-    uint32_t rc[PER];
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const uint32_t c = base + lane + 32u * k;
-      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : 0xFFFFFFFFu;
-    }
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const uint32_t c = base + lane + 32u * k;
-      if (rc[k] != c) continue;  // not a root run: no entry of its own
-      const uint32_t R = gfind(p.E, node0 + c, node_count(p), p.ctr, limit_of(p.budget, kFindLimit));
-      if (R == kBadNode) {
-        p.label[node0 + c] = 0u;
-        continue;
-      }
-      const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
-      const uint32_t w = key >> 5;
-      uint32_t lab = 0;
-      if (w < p.nwords) {
-        const uint32_t below = __ldg(p.bitmap + w) & ((1u << (key & 31)) - 1u);
-        lab = __ldg(p.prefix + w) + __popc(below) + 1u - rank0;
-      } else {
-        atomicOr(&p.ctr->err, ERR_INDEX);
-      }
-      p.label[node0 + c] = lab;
-    }
-  }
-  __syncwarp();
-  for (uint32_t base = 0; base < C; base += 32 * PER) {
-    uint32_t rc[PER], lab[PER];
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const uint32_t c = base + lane + 32u * k;
-      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : c;
-    }
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const uint32_t c = base + lane + 32u * k;
-      lab[k] = (c < C && rc[k] != c && rc[k] < C) ? p.label[node0 + rc[k]] : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const uint32_t c = base + lane + 32u * k;
-      if (c >= C || rc[k] == c) continue;
-      if (rc[k] < C) p.label[node0 + c] = lab[k];
-      else atomicOr(&p.ctr->err, ERR_INDEX);
-    }
-  }
+  resolve_tile(p, tile, threadIdx.x & 31);
 }
 
 static void launch_resolve_all(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {

@@ -26,28 +26,32 @@ __device__ __forceinline__ void merge_tile_edges(const LabelArgs& p, int64_t til
   }
 }
 
-// K2 of the 32 tiles [t0, t0 + 32), by one warp: their edges are numbered one
-// after the other (a warp scan of the tiles' edge counts) and taken 32 at a
-// time, one per lane, so every round of dependent loads serves 32 edges
-// (a tile has a few dozen edges; one warp per tile leaves most lanes of its
-// last round idle).
+// K2 of the G tiles [t0, t0 + G), by one warp: their edges are numbered one
+// after the other (a scan of the tiles' edge counts over lanes 0..G-1) and
+// taken 32 at a time, one per lane, so every round of dependent loads serves
+// 32 edges (a tile has a few dozen edges; one warp per tile leaves most lanes
+// of its last round idle).  G stays small so that the grid still has a warp
+// for every few tiles.
+constexpr int kMergeGroup = 4;
+template <int G>
 __device__ __forceinline__ void merge_group_edges(const LabelArgs& p, int64_t t0, int lane) {
+  static_assert(G >= 1 && G <= 32 && (G & (G - 1)) == 0, "group of 1..32 tiles, a power of two");
   const int64_t tile = t0 + lane;
-  const uint32_t n = tile < p.ntiles ? p.tinfo[tile].nedges : 0u;
+  const uint32_t n = (lane < G && tile < p.ntiles) ? p.tinfo[tile].nedges : 0u;
   uint32_t incl = n;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
+  for (int o = 1; o < G; o <<= 1) {
     const uint32_t y = __shfl_up_sync(FULL, incl, o);
     if (lane >= o) incl += y;
   }
   const uint32_t excl = incl - n;
-  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  const uint32_t total = __shfl_sync(FULL, incl, G - 1);
   for (uint32_t base = 0; base < total; base += 32) {
     const uint32_t e = base + lane;
-    // the lane (tile) whose edge range holds e: the last lane with excl <= e
+    // the tile whose edge range holds e: the last of lanes 0..G-1 with excl <= e
     int lo = 0;
 #pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
+    for (int step = G / 2; step > 0; step >>= 1) {
       const uint32_t ex = __shfl_sync(FULL, excl, lo + step);
       if (ex <= e) lo += step;
     }
@@ -188,6 +192,67 @@ __device__ __forceinline__ void scan_down_chunk(const uint32_t* bitmap, int64_t 
     run += c[k];
   }
   __syncthreads();  // the block's shared words are free for its next chunk
+}
+
+// Label of every run of one tile, by one warp: 1 + the rank of its
+// component root's key among the surviving keys (minus the keys of the volumes
+// before it, in a batch), into the per-run slots p.label.  The root runs
+// (whose component id is their own index) are resolved first, then every
+// other run copies its root run's label; eight runs per lane are in flight at
+// once.
+__device__ __forceinline__ void resolve_tile(const LabelArgs& p, int64_t tile, int lane) {
+  uint32_t C = p.tinfo[tile].C;
+  if (C > kTV) C = kTV;
+  const uint32_t node0 = (uint32_t)(tile * kTV);
+  const uint32_t rank0 = p.vols ? (uint32_t)p.vols[p.tile_vol[tile]].rank0 : 0u;
+  constexpr int PER = 8;
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (rc[k] != c) continue;  // not a root run: no entry of its own
+      const uint32_t R = gfind(p.E, node0 + c, node_count(p), p.ctr, limit_of(p.budget, kFindLimit));
+      uint32_t lab = 0;
+      if (R != kBadNode) {
+        const uint32_t key = (uint32_t)(gload(p.E + R) >> 32);
+        const uint32_t w = key >> 5;
+        if (w < p.nwords) {
+          const uint32_t below = __ldg(p.bitmap + w) & ((1u << (key & 31)) - 1u);
+          lab = __ldg(p.prefix + w) + __popc(below) + 1u - rank0;
+        } else {
+          atomicOr(&p.ctr->err, ERR_INDEX);
+        }
+      }
+      p.label[node0 + c] = lab;
+    }
+  }
+  __syncwarp();
+  for (uint32_t base = 0; base < C; base += 32 * PER) {
+    uint32_t rc[PER], lab[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      rc[k] = c < C ? (uint32_t)p.rcomp[node0 + c] : c;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      lab[k] = (c < C && rc[k] != c && rc[k] < C) ? p.label[node0 + rc[k]] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t c = base + lane + 32u * k;
+      if (c >= C || rc[k] == c) continue;
+      if (rc[k] < C) p.label[node0 + c] = lab[k];
+      else atomicOr(&p.ctr->err, ERR_INDEX);
+    }
+  }
 }
 
 // ------------------------------------------------------------ batches

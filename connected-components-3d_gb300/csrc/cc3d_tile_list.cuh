@@ -209,8 +209,8 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   // per box row: the tile holding its 32 voxels and the row's index inside
   // that tile; the same-owner box row before it (one back in y, else in z;
   // 255: none)
-  __shared__ uint32_t rtile[NRB];
-  __shared__ unsigned char rloc[NRB], rprev[NRB];
+  __shared__ unsigned char rloc[NRB], rprev[NRB], rown[NRB];
+  __shared__ TileGeo sgeo;  // the tile's place in its volume (one warp works it out)
   // the tile's list: one entry per voxel that has unions to run,
   // (needy << 14) | (row-level pairs << 11) | (tile row << 5) | x; in phase C
   // each warp's slice holds the run heads of its rows
@@ -233,10 +233,8 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   __shared__ unsigned int edge_fill;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const TileGeo g = tile_geo(p, tile);
   const uint32_t utile = (uint32_t)tile;  // tile ids and node ids fit 32 bits
   const uint32_t node0 = utile * (uint32_t)kTV;
-  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
   const uint32_t lt = (1u << lane) - 1u;
   const int llim = limit_of(p.budget, kLocalLimit);
 
@@ -261,19 +259,26 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   };
 
   // ---- phase 0: the box arrives while the node bases are set up
-  if (tid == 0) {
-    local_err = 0;
-    edge_fill = 0;
-    list_fill = 0;
-    if (use_tma) {
-      mbar_init(&tbar, 1);
-      fence_mbar_init();
-      fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&tbar, (uint32_t)(NRB * W * sizeof(T)));
-      tma_load_3d(box, tmap, &tbar, (int)(x0 - PADX), (int)(y0 - 1), (int)(z0 - HZ));
+  if (warp == 0) {
+    const TileGeo gg = tile_geo(p, tile);
+    if (lane == 0) {
+      sgeo = gg;
+      local_err = 0;
+      edge_fill = 0;
+      list_fill = 0;
+      if (use_tma) {
+        mbar_init(&tbar, 1);
+        fence_mbar_init();
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&tbar, (uint32_t)(NRB * W * sizeof(T)));
+        tma_load_3d(box, tmap, &tbar, (int)(gg.tx * kTX - PADX), (int)((int64_t)gg.ty * TY - 1),
+                    (int)((int64_t)gg.tz * TZ - HZ));
+      }
     }
   }
   if (!use_tma) {
+    const TileGeo g = tile_geo(p, tile);
+    const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
     const T* in = static_cast<const T*>(g.in);
     for (int rb = warp; rb < NRB; rb += NW) {
       const int by = rb % BY, bz = rb / BY;
@@ -304,8 +309,7 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
     const int ly = by == 0 ? TY - 1 : (by == BY - 1 ? 0 : by - 1);
     const int lz = bz < HZ ? TZ - 1 : bz - HZ;
     rloc[rb] = (unsigned char)(ly + TY * lz);
-    // (rows outside the volume hold no foreground, so their tile id is unused)
-    rtile[rb] = utile + (uint32_t)dy * (uint32_t)g.ntx + (uint32_t)dz * ((uint32_t)g.ntx * (uint32_t)g.nty);
+    rown[rb] = (unsigned char)((dy + 1) + 3 * (dz + 1));
     // which tile holds a box row: its y and z offsets from this tile
     auto owner = [&](int r) -> int {
       const int b = r % BY, c = r / BY;
@@ -326,6 +330,9 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
     }
   }
   __syncthreads();
+  const TileGeo g = sgeo;
+  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
+  (void)x0;
 
   // ---- phase A: run masks of every box row; run heads become nodes; the
   // provisional-label estimate (cc3d/cc3d.hpp:287-315) on the tile rows
@@ -618,6 +625,13 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   // in y, else in z) relates to it and joined the same component: both lie
   // in one component of their own tile, so that edge would repeat
   uint2* edges = p.edges + (size_t)utile * p.edge_slots;
+  // the tile holding box row rb (rows outside the volume hold no foreground,
+  // so their tile id is unused)
+  const uint32_t ntx = (uint32_t)g.ntx, ntxy = ntx * (uint32_t)g.nty;
+  auto rtile = [&](int rb) -> uint32_t {
+    const int own = rown[rb];
+    return utile + (uint32_t)(own % 3 - 1) * ntx + (uint32_t)(own / 3 - 1) * ntxy;
+  };
   constexpr int NCC = (2 * NRB + 31) / 32;  // 32-voxel chunks of the two halo columns
   constexpr int NHW = (NHR + 31) / 32;      // warps that take the halo rows, one lane per row
   static_assert(NHW + 1 <= NW, "warps left for the halo columns");
@@ -639,7 +653,7 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
         }
         const unsigned slot = atomicAdd(&edge_fill, 1u);
         if (slot < p.edge_slots)
-          edges[slot] = make_uint2(node0 + rid_of(r), (rtile[rb] * (uint32_t)kRowsPerTile + rloc[rb]) * 32u + x);
+          edges[slot] = make_uint2(node0 + rid_of(r), (rtile(rb) * (uint32_t)kRowsPerTile + rloc[rb]) * 32u + x);
       }
     }
   } else {
@@ -663,7 +677,7 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
             // (x0 + 32) of the row's tile, at x 31 or 0 of that tile
             if (has)
               e = make_uint2(node0 + rid_of(r),
-                             ((rtile[rb] + (side ? 1u : 0xFFFFFFFFu)) * (uint32_t)kRowsPerTile + rloc[rb]) * 32u +
+                             ((rtile(rb) + (side ? 1u : 0xFFFFFFFFu)) * (uint32_t)kRowsPerTile + rloc[rb]) * 32u +
                                  (side ? 0u : 31u));
           }
         }
