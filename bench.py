@@ -449,7 +449,7 @@ def run_gpu(args, world, rank, local):
         batch = measure_batch(batch_stream(BATCH_VOLUMES), max(3, min(args.steps, 10)), 3)
         batch["costmodel"] = costmodel_regret()
 
-    launches_per_step = 8  # tile pass, edge merge, 3 scan kernels + tile reduction, resolve, write
+    launches_per_step = 6  # tile pass, edge merge, 3 numbering-scan kernels, label writer
     line = {
         "metric": METRIC, "value": value, "unit": "GVoxels/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "cc3d_gpu.h"
@@ -75,6 +76,7 @@ struct PersistState {
   int grid = 0;
 };
 thread_local std::map<int, PersistState> g_persist;
+std::mutex g_persist_args_mu;
 thread_local int g_batch_mode = CC3D_BATCH_PERSISTENT;
 
 void drop_graph(BatchState& b) {
@@ -593,7 +595,12 @@ static int label_batch_persistent(const cc3d_gpu_volume* vols, int n, int dtype,
     b.hdr = (void*)dh;
     b.grid = grid;
   }
+  // the kernels read their arguments from one constant-memory copy per
+  // dtype: batches of several host threads take turns
+  std::lock_guard<std::mutex> args_lock(g_persist_args_mu);
   CKB(cudaMemcpyAsync(b.dev, b.host, up_bytes, cudaMemcpyHostToDevice, s));
+  CKB(dtype == CC3D_U8 ? persistent_args_u8(&h->a, s)
+                       : dtype == CC3D_U16 ? persistent_args_u16(&h->a, s) : persistent_args_u32(&h->a, s));
   CKB(cudaGraphLaunch(b.exec, s));
   BatchResult* hres = (BatchResult*)(b.host + up_bytes);
   CKB(cudaMemcpyAsync(hres, b.dev + o_res, nv * sizeof(BatchResult), cudaMemcpyDeviceToHost, s));

@@ -17,9 +17,10 @@
 //   8  labels                     one block per tile (write_tile)
 //
 // Every argument -- the buffers, the tile and word counts, the volume
-// descriptors -- comes from a header in device memory uploaded before the
-// launch, so the launch itself does not depend on the batch's layout: the
-// host captures it once into a CUDA graph and replays it for every batch.
+// descriptors -- comes from device memory written before the launch (the
+// labelling arguments in constant memory, the rest in a header), so the
+// launch itself does not depend on the batch's layout: the host captures it
+// once into a CUDA graph and replays it for every batch.
 // Every grid barrier is bounded: a block that waits too long sets ERR_WAIT
 // and the kernel ends (the host reports the error).
 #pragma once
@@ -29,8 +30,17 @@
 
 namespace cc3dgpu {
 
+// The labelling arguments of the batch being labelled (one copy per
+// translation unit that includes this header: each dtype's kernels read their
+// own, written by persistent_args_* of the same unit before each launch).
+static __constant__ LabelArgs c_batch_args;
+
+inline cudaError_t set_persistent_args(const LabelArgs* a, cudaStream_t s) {
+  return cudaMemcpyToSymbolAsync(c_batch_args, a, sizeof(LabelArgs), 0, cudaMemcpyHostToDevice, s);
+}
+
 struct PersistentHeader {
-  LabelArgs a;        // a.ctr points at ctr below; a.vols, a.tile_vol into the arena
+  LabelArgs a;        // host staging of c_batch_args: a.ctr points at ctr below
   int64_t nwords;     // bitmap words of the whole batch
   int64_t nblocks;    // scan chunks
   uint32_t* bsum;     // [nblocks + 1] chunk sums
@@ -79,12 +89,7 @@ template <typename T, int CONN>
 __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHeader* hdr) {
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
   constexpr int TY = D3 ? 8 : 64, TZ = D3 ? 8 : 1;
-  __shared__ LabelArgs sp;
-  static_assert(sizeof(LabelArgs) % 4 == 0, "word copy");
-  for (int i = threadIdx.x; i < (int)(sizeof(LabelArgs) / 4); i += blockDim.x)
-    reinterpret_cast<uint32_t*>(&sp)[i] = reinterpret_cast<const uint32_t*>(&hdr->a)[i];
-  __syncthreads();
-  const LabelArgs& p = sp;
+  const LabelArgs& p = c_batch_args;
   const int lane = threadIdx.x & 31;
   const int nv = hdr->nvol;
   const int64_t ntiles = p.ntiles, nwords = hdr->nwords, nblocks = hdr->nblocks;

@@ -127,6 +127,10 @@ cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t 
 const void* persistent_kernel_u8(int conn);
 const void* persistent_kernel_u16(int conn);
 const void* persistent_kernel_u32(int conn);
+// write the labelling arguments the persistent kernels of a dtype read
+cudaError_t persistent_args_u8(const LabelArgs* a, cudaStream_t s);
+cudaError_t persistent_args_u16(const LabelArgs* a, cudaStream_t s);
+cudaError_t persistent_args_u32(const LabelArgs* a, cudaStream_t s);
 
 // statistics (cc3d_stats.cu)
 struct StatsArgs {
