@@ -46,10 +46,13 @@ struct PersistentHeader {
   uint32_t* bsum;     // [nblocks + 1] chunk sums
   BatchResult* res;   // [nvol]
   int nvol;
-  unsigned bar_count; // grid barrier: blocks arrived, generation
-  unsigned bar_gen;
-  unsigned pad;
-  Counters ctr;
+  // the counters and the two grid-barrier words each on cache lines of their
+  // own: every waiting block polls the generation word, and traffic on its
+  // line must not slow the counters' atomics or the header's reads
+  alignas(128) Counters ctr;
+  alignas(128) unsigned bar_count;  // blocks arrived at the current barrier
+  alignas(128) unsigned bar_gen;    // barrier generation
+  unsigned tail_pad[31];
 };
 
 constexpr int kBarrierLimit = 1 << 22;  // polls of one grid barrier before giving up
@@ -75,7 +78,7 @@ __device__ __forceinline__ bool grid_barrier(PersistentHeader* h) {
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(256);
       }
     }
     __threadfence();
@@ -93,6 +96,8 @@ __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHead
   const int lane = threadIdx.x & 31;
   const int nv = hdr->nvol;
   const int64_t ntiles = p.ntiles, nwords = hdr->nwords, nblocks = hdr->nblocks;
+  uint32_t* const bsum = hdr->bsum;
+  BatchResult* const res = hdr->res;
   const int64_t gw = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
   const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
 
@@ -110,14 +115,14 @@ __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHead
   if (!grid_barrier(hdr)) return;
   // 3-5: numbering scan
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
-    scan_reduce_chunk(p.bitmap, nwords, hdr->bsum, p.tinfo, ntiles, p.ctr, b, nblocks);
+    scan_reduce_chunk(p.bitmap, nwords, bsum, p.tinfo, ntiles, p.ctr, b, nblocks);
   if (!grid_barrier(hdr)) return;
-  if (blockIdx.x == 0) scan_chunk_sums<kThreads>(hdr->bsum, nblocks, p.ctr);
+  if (blockIdx.x == 0) scan_chunk_sums<kThreads>(bsum, nblocks, p.ctr);
   if (!grid_barrier(hdr)) return;
-  for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) scan_down_chunk(p.bitmap, nwords, hdr->bsum, p.prefix, b);
+  for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) scan_down_chunk(p.bitmap, nwords, bsum, p.prefix, b);
   if (!grid_barrier(hdr)) return;
   // 6: per-volume results
-  for (int64_t v = gw; v < nv; v += nwarps) finalize_volume(p, (int)v, nv, nwords, hdr->res, lane);
+  for (int64_t v = gw; v < nv; v += nwarps) finalize_volume(p, (int)v, nv, nwords, res, lane);
   if (!grid_barrier(hdr)) return;
   // 7: run labels, one warp per tile
   for (int64_t t = gw; t < ntiles; t += nwarps) resolve_tile(p, t, lane);

@@ -18,7 +18,8 @@ import __graft_entry__ as entry
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ("list/8x8", "runs/8x8", "list/4x16", "runs/4x16", "list/16x4", "runs/16x4")
+VARIANTS = ("list/8x8", "runs/8x8", "list/4x16", "runs/4x16", "list/16x4", "runs/16x4", "list/16x4/plain",
+            "runs/8x8/plain")
 
 
 @pytest.fixture(scope="module")

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module", params=["list/8x8", "runs/8x8", "list/4x16", "runs/4x16", "list/16x4",
-                                        "runs/16x4"])
+                                        "runs/16x4", "list/8x8/plain", "runs/16x4/plain"])
 def cc3d(request):
     """The package with one tile-pass configuration selected: every parity
     test runs once per configuration."""
