@@ -186,7 +186,7 @@ int check_device_errors(unsigned err) {
               (err & ERR_FIND_BUDGET) ? "find budget " : "",
               (err & ERR_EDGE_OVERFLOW) ? "edge buffer overflow " : "",
               (err & ERR_LOCAL_BUDGET) ? "tile union budget " : "",
-              (err & ERR_WAIT) ? "input copy never completed " : "",
+              (err & ERR_WAIT) ? "a bounded wait ran out (input copy or grid barrier) " : "",
               (err & ERR_INDEX) ? "index range check" : "");
 }
 
