@@ -7,14 +7,16 @@
 // barrier between stages:
 //
 //   0  tile -> volume map         one block per volume
-//   1  tile pass                  one block per tile (tile_list_tile)
+//   1  tile pass                  one block per tile (tile_list_tile), tiles
+//                                 taken from a work queue
 //   2  edge merges                one warp per 4 tiles (merge_group_edges)
 //   3  chunk popcounts            one block per bitmap chunk
 //   4  scan of the chunk sums     block 0
 //   5  word prefixes              one block per bitmap chunk
 //   6  per-volume results         one warp per volume (finalize_volume)
-//   7  run labels                 one warp per tile (resolve_tile)
-//   8  labels                     one block per tile (write_tile)
+//   7  labels                     one warp per tile: its run labels
+//                                 (resolve_tile), then its rows
+//                                 (write_tile_warp)
 //
 // Every argument -- the buffers, the tile and word counts, the volume
 // descriptors -- comes from device memory written before the launch (the
@@ -52,7 +54,10 @@ struct PersistentHeader {
   alignas(128) Counters ctr;
   alignas(128) unsigned bar_count;  // blocks arrived at the current barrier
   alignas(128) unsigned bar_gen;    // barrier generation
-  unsigned tail_pad[31];
+  // the tile pass's work queue: the next tile a block takes (zero in the
+  // uploaded header)
+  alignas(128) unsigned long long next_tile;
+  unsigned tail_pad[30];
 };
 
 constexpr int kBarrierLimit = 1 << 22;  // polls of one grid barrier before giving up
@@ -88,51 +93,79 @@ __device__ __forceinline__ bool grid_barrier(PersistentHeader* h) {
   return s_ok != 0;
 }
 
+// A block's walk over the n items of a work queue: thread 0 takes the next
+// item (one atomicAdd) while the block works on the current one.  A queue,
+// not a fixed share per block: the SM's scheduler favours its older blocks,
+// so with fixed shares the younger blocks of every SM finish last and the
+// SM idles meanwhile.  The body must hold a block barrier that every thread
+// reaches (the tile pass has several): thread 0 writes the next item before
+// it, the others read it after it, and everyone has read the current item
+// before thread 0 can overwrite that slot one item later.
+template <typename F>
+__device__ __forceinline__ void drain_queue(unsigned long long* q, int64_t n, F&& body) {
+  __shared__ long long s_item[2];
+  if (threadIdx.x == 0) s_item[0] = (long long)atomicAdd(q, 1ull);
+  __syncthreads();
+  for (int k = 0;; k ^= 1) {
+    const long long t = s_item[k];
+    if (t >= n) break;
+    if (threadIdx.x == 0) s_item[k ^ 1] = (long long)atomicAdd(q, 1ull);
+    body((int64_t)t);
+  }
+}
+
 template <typename T, int CONN>
 __global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHeader* hdr) {
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
   constexpr int TY = D3 ? 8 : 64, TZ = D3 ? 8 : 1;
   const LabelArgs& p = c_batch_args;
   const int lane = threadIdx.x & 31;
-  const int nv = hdr->nvol;
-  const int64_t ntiles = p.ntiles, nwords = hdr->nwords, nblocks = hdr->nblocks;
-  uint32_t* const bsum = hdr->bsum;
-  BatchResult* const res = hdr->res;
-  const int64_t gw = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+  // (the header's fields are read where a stage needs them, not held in
+  // registers across the stages: the tile pass needs every register)
+  auto warp_id = [] { return (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); };
+  auto warps = [] { return (int64_t)gridDim.x * (kThreads / 32); };
 
   // 0: the volume of every tile
-  for (int v = blockIdx.x; v < nv; v += gridDim.x) {
-    const int64_t t0 = p.vols[v].tile0, t1 = v + 1 < nv ? p.vols[v + 1].tile0 : ntiles;
-    for (int64_t t = t0 + threadIdx.x; t < t1; t += kThreads) const_cast<uint32_t*>(p.tile_vol)[t] = (uint32_t)v;
+  {
+    const int nv = hdr->nvol;
+    for (int v = blockIdx.x; v < nv; v += gridDim.x) {
+      const int64_t t0 = p.vols[v].tile0, t1 = v + 1 < nv ? p.vols[v + 1].tile0 : p.ntiles;
+      for (int64_t t = t0 + threadIdx.x; t < t1; t += kThreads) const_cast<uint32_t*>(p.tile_vol)[t] = (uint32_t)v;
+    }
   }
   if (!grid_barrier(hdr)) return;
-  // 1: tile pass
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_list_tile<T, CONN, TY, TZ, MODE_MULTI>(p, nullptr, 0, t);
+  // 1: tile pass, tiles in order from the queue
+  drain_queue(&hdr->next_tile, p.ntiles,
+              [&](int64_t t) { tile_list_tile<T, CONN, TY, TZ, MODE_MULTI, true>(p, nullptr, 0, t); });
   if (!grid_barrier(hdr)) return;
   // 2: edge merges
-  for (int64_t g = gw; g * kMergeGroup < ntiles; g += nwarps) merge_group_edges<kMergeGroup>(p, g * kMergeGroup, lane);
+  for (int64_t g = warp_id(); g * kMergeGroup < p.ntiles; g += warps())
+    merge_group_edges<kMergeGroup>(p, g * kMergeGroup, lane);
   if (!grid_barrier(hdr)) return;
   // 3-5: numbering scan
-  for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
-    scan_reduce_chunk(p.bitmap, nwords, bsum, p.tinfo, ntiles, p.ctr, b, nblocks);
+  for (int64_t b = blockIdx.x; b < hdr->nblocks; b += gridDim.x)
+    scan_reduce_chunk(p.bitmap, hdr->nwords, hdr->bsum, p.tinfo, p.ntiles, p.ctr, b, hdr->nblocks);
   if (!grid_barrier(hdr)) return;
-  if (blockIdx.x == 0) scan_chunk_sums<kThreads>(bsum, nblocks, p.ctr);
+  if (blockIdx.x == 0) scan_chunk_sums<kThreads>(hdr->bsum, hdr->nblocks, p.ctr);
   if (!grid_barrier(hdr)) return;
-  for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) scan_down_chunk(p.bitmap, nwords, bsum, p.prefix, b);
+  for (int64_t b = blockIdx.x; b < hdr->nblocks; b += gridDim.x)
+    scan_down_chunk(p.bitmap, hdr->nwords, hdr->bsum, p.prefix, b);
   if (!grid_barrier(hdr)) return;
   // 6: per-volume results
-  for (int64_t v = gw; v < nv; v += nwarps) finalize_volume(p, (int)v, nv, nwords, res, lane);
+  {
+    const int nv = hdr->nvol;
+    for (int64_t v = warp_id(); v < nv; v += warps()) finalize_volume(p, (int)v, nv, hdr->nwords, hdr->res, lane);
+  }
   if (!grid_barrier(hdr)) return;
-  // 7: run labels, one warp per tile
-  for (int64_t t = gw; t < ntiles; t += nwarps) resolve_tile(p, t, lane);
-  if (!grid_barrier(hdr)) return;
-  // 8: the labels written, one block per tile (write_tile), in the volume's
-  // output type
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // 7: the labels, one warp per tile: the tile's run labels (resolve_tile),
+  // then its rows in the volume's output type (write_tile_warp)
+  for (int64_t t = warp_id(); t < p.ntiles; t += warps()) {
+    resolve_tile(p, t, lane);
+    __syncwarp();
     const VolGeo& v = p.vols[p.tile_vol[t]];
-    if (v.out_code == 2) write_tile<uint16_t, TY, TZ>(p, t, static_cast<uint16_t*>(v.out));
-    else write_tile<uint32_t, TY, TZ>(p, t, static_cast<uint32_t*>(v.out));
+    if (v.out_code == 2) write_tile_warp<uint16_t, TY, TZ>(p, t, v, static_cast<uint16_t*>(v.out), lane);
+    else write_tile_warp<uint32_t, TY, TZ>(p, t, v, static_cast<uint32_t*>(v.out), lane);
+    __syncwarp();
   }
 }
 

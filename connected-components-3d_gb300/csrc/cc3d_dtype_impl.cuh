@@ -208,14 +208,16 @@ cudaError_t launch_k1_runs(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
 }
 
 // the list pass (multilabel and binary relations): one CTA of 256 threads per
-// tile, its box staged by one TMA copy
+// tile, its box staged by one TMA copy where the volume allows (else by
+// plain loads, a kernel of its own)
 template <typename T, int CONN, int TY, int TZ, int MODE>
 cudaError_t launch_k1_list(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
   using B = TileBox<CONN, TY, TZ>;
   CUtensorMap map;
   const int use_tma =
       ntiles > 0 ? encode_input_map<T>(a, (uint32_t)BoxRow<T>::W, (uint32_t)B::BY, (uint32_t)B::BZ, &map) : 0;
-  k_tile_list<T, CONN, TY, TZ, MODE><<<(unsigned)ntiles, kThreads, 0, s>>>(a, map, use_tma);
+  if (use_tma) k_tile_list<T, CONN, TY, TZ, MODE, true><<<(unsigned)ntiles, kThreads, 0, s>>>(a, map);
+  else k_tile_list<T, CONN, TY, TZ, MODE, false><<<(unsigned)ntiles, kThreads, 0, s>>>(a, map);
   return cudaGetLastError();
 }
 

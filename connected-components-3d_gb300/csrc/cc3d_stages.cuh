@@ -1,7 +1,7 @@
 // cc3d_stages.cuh -- the element-type independent stages after the tile pass,
 // written as device functions of one warp or one block, so that the staged
 // kernels (cc3d_core.cu: one launch per stage) and the persistent batch kernel
-// (cc3d_batch_persistent.cu: every stage in one launch) run the same code.
+// (cc3d_batch_persistent.cuh: every stage in one launch) run the same code.
 #pragma once
 
 #include "cc3d_internal.h"
@@ -251,6 +251,70 @@ __device__ __forceinline__ void resolve_tile(const LabelArgs& p, int64_t tile, i
       if (c >= C || rc[k] == c) continue;
       if (rc[k] < C) p.label[node0 + c] = lab[k];
       else atomicOr(&p.ctr->err, ERR_INDEX);
+    }
+  }
+}
+
+// The labels of tile `tile` of a batch volume, by one warp, from the run
+// labels resolve_tile left in p.label (read with coherent loads: they were
+// written by this kernel).  Four rows per step: lane = 8 * (row of the four)
+// + group, and a lane writes voxels 4 * group .. 4 * group + 3 of its row with
+// one vector store where the row allows it.  A warp per tile, not a block,
+// so that 48 tiles per SM have their dependent loads in flight at once.
+template <typename OUT, int TY, int TZ>
+__device__ __forceinline__ void write_tile_warp(const LabelArgs& p, int64_t tile, const VolGeo& v, OUT* out,
+                                                int lane) {
+  static_assert(sizeof(OUT) == 2 || sizeof(OUT) == 4, "batch outputs are uint16 or uint32");
+  static_assert(TY * TZ == kRowsPerTile, "rows per tile");
+  uint32_t C = p.tinfo[tile].C;
+  if (C > kTV) {
+    if (lane == 0) atomicOr(&p.ctr->err, ERR_INDEX);
+    C = kTV;
+  }
+  const uint32_t local = (uint32_t)(tile - v.tile0);
+  const uint32_t ntx = (uint32_t)v.ntx, nty = (uint32_t)v.nty;
+  const uint32_t rest = local / ntx, tz = rest / nty;
+  const int64_t x0 = (int64_t)(local - rest * ntx) * kTX;
+  const int64_t y0 = (int64_t)(rest - tz * nty) * TY, z0 = (int64_t)tz * TZ;
+  const uint32_t* lab = p.label + tile * kTV;
+  const uint2 ma = p.rmask[tile * kRowsPerTile + lane], mb = p.rmask[tile * kRowsPerTile + 32 + lane];
+  const uint32_t ra = p.rrow[tile * kRowsPerTile + lane], rb = p.rrow[tile * kRowsPerTile + 32 + lane];
+  const int g4 = (lane & 7) * 4, rq = lane >> 3;
+  const int64_t sx = v.sx, sy = v.sy, sz = v.sz, xg = x0 + g4, plane = sx * sy;
+  const bool vec = (sx & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & (4 * sizeof(OUT) - 1)) == 0;
+  OUT* const base_ptr = out + z0 * plane + y0 * sx + xg;
+#pragma unroll 1
+  for (int r0 = 0; r0 < kRowsPerTile; r0 += 4) {
+    const int ri = r0 + rq;
+    const uint32_t F = __shfl_sync(FULL, r0 < 32 ? ma.x : mb.x, ri & 31);
+    const uint32_t S = __shfl_sync(FULL, r0 < 32 ? ma.y : mb.y, ri & 31);
+    const uint32_t b = __shfl_sync(FULL, r0 < 32 ? ra : rb, ri & 31);
+    OUT o[4];
+    // run of voxel g4 (the last run start at or before it), then of the next three
+    int k = __popc(S & lanemask_le(g4)) - 1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i) k += (S >> (g4 + i)) & 1u;
+      o[i] = OUT(0);
+      if ((F >> (g4 + i)) & 1u) {
+        const uint32_t r = b + (uint32_t)k;
+        if (k >= 0 && r < C) o[i] = (OUT)lab[r];
+        else atomicOr(&p.ctr->err, ERR_INDEX);
+      }
+    }
+    const int ly = ri % TY, lz = ri / TY;
+    if (y0 + ly >= sy || z0 + lz >= sz) continue;
+    OUT* dst = base_ptr + lz * plane + ly * sx;
+    if (vec && xg + 3 < sx) {
+      if constexpr (sizeof(OUT) == 2)
+        *reinterpret_cast<uint2*>(dst) =
+            make_uint2((uint32_t)o[0] | ((uint32_t)o[1] << 16), (uint32_t)o[2] | ((uint32_t)o[3] << 16));
+      else
+        *reinterpret_cast<uint4*>(dst) = make_uint4((uint32_t)o[0], (uint32_t)o[1], (uint32_t)o[2], (uint32_t)o[3]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (xg + i < sx) dst[i] = o[i];
     }
   }
 }

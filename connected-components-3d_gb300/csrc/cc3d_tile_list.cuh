@@ -167,7 +167,8 @@ static __device__ __noinline__ int list_unions(const uint32_t* q, int n, PT* par
   return err;
 }
 
-template <typename T, int CONN, int TY, int TZ, int MODE>
+// LOOP: the caller labels tile after tile in one block (the persistent batch)
+template <typename T, int CONN, int TY, int TZ, int MODE, bool LOOP = false>
 __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtensorMap* tmap, int use_tma,
                                                int64_t tile) {
   static_assert(MODE == MODE_MULTI || MODE == MODE_BINARY, "multilabel or binary relation");
@@ -232,7 +233,14 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   __shared__ unsigned int local_err;
   __shared__ unsigned int edge_fill;
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // In a loop over tiles the thread index passes through an empty asm, so
+  // that what is derived from it is worked out again for every tile: the
+  // block would otherwise keep all of it live across the whole loop and
+  // spill.  (A single tile keeps the plain form, which issues fewer
+  // instructions.)
+  int tid_in = threadIdx.x;
+  if constexpr (LOOP) asm volatile("" : "+r"(tid_in));
+  const int tid = tid_in, lane = tid & 31, warp = tid >> 5;
   const uint32_t utile = (uint32_t)tile;  // tile ids and node ids fit 32 bits
   const uint32_t node0 = utile * (uint32_t)kTV;
   const uint32_t lt = (1u << lane) - 1u;
@@ -754,10 +762,13 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
   }
 }
 
-template <typename T, int CONN, int TY, int TZ, int MODE>
+// TMA: the box arrives by one TMA copy (else by plain loads); two kernels, so
+// that each holds only its own way of loading and keeps its registers for the
+// phases after it
+template <typename T, int CONN, int TY, int TZ, int MODE, bool TMA>
 __global__ void __launch_bounds__(kThreads, 6)
-k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap, int use_tma) {
-  tile_list_tile<T, CONN, TY, TZ, MODE>(p, &tmap, use_tma, p.tile_base + blockIdx.x);
+k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap) {
+  tile_list_tile<T, CONN, TY, TZ, MODE>(p, &tmap, TMA ? 1 : 0, p.tile_base + blockIdx.x);
 }
 
 }  // namespace cc3dgpu
