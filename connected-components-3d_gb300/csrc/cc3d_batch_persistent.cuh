@@ -55,9 +55,9 @@ struct PersistentHeader {
   alignas(128) unsigned bar_count;  // blocks arrived at the current barrier
   alignas(128) unsigned bar_gen;    // barrier generation
   // the tile pass's work queue: the next tile a block takes (zero in the
-  // uploaded header)
-  alignas(128) unsigned long long next_tile;
-  unsigned tail_pad[30];
+  // uploaded header; a batch has fewer than 2^21 tiles)
+  alignas(128) unsigned next_tile;
+  unsigned tail_pad[31];
 };
 
 constexpr int kBarrierLimit = 1 << 22;  // polls of one grid barrier before giving up
@@ -93,29 +93,38 @@ __device__ __forceinline__ bool grid_barrier(PersistentHeader* h) {
   return s_ok != 0;
 }
 
-// A block's walk over the n items of a work queue: thread 0 takes the next
-// item (one atomicAdd) while the block works on the current one.  A queue,
-// not a fixed share per block: the SM's scheduler favours its older blocks,
-// so with fixed shares the younger blocks of every SM finish last and the
-// SM idles meanwhile.  The body must hold a block barrier that every thread
-// reaches (the tile pass has several): thread 0 writes the next item before
-// it, the others read it after it, and everyone has read the current item
-// before thread 0 can overwrite that slot one item later.
+// A block's walk over the n items of a work queue.  A queue, not a fixed
+// share per block: the SM's scheduler favours its older blocks, so with fixed
+// shares the younger blocks of every SM finish last and the SM idles
+// meanwhile.  Thread 0 takes items two ahead of their use: the item it
+// publishes (to shared memory) before the body was fetched one body earlier,
+// so no thread waits for the atomic.  The body must hold a block barrier that
+// every thread reaches (the tile pass has several): thread 0 writes the next
+// item before it, the others read it after it, and everyone has read the
+// current item before thread 0 overwrites that slot one item later.
 template <typename F>
-__device__ __forceinline__ void drain_queue(unsigned long long* q, int64_t n, F&& body) {
-  __shared__ long long s_item[2];
-  if (threadIdx.x == 0) s_item[0] = (long long)atomicAdd(q, 1ull);
+__device__ __forceinline__ void drain_queue(unsigned* q, int64_t n, F&& body) {
+  __shared__ unsigned s_item[2];
+  unsigned ahead = 0;
+  if (threadIdx.x == 0) {
+    s_item[0] = atomicAdd(q, 1u);
+    ahead = atomicAdd(q, 1u);
+  }
   __syncthreads();
   for (int k = 0;; k ^= 1) {
-    const long long t = s_item[k];
-    if (t >= n) break;
-    if (threadIdx.x == 0) s_item[k ^ 1] = (long long)atomicAdd(q, 1ull);
+    const unsigned t = s_item[k];
+    if ((int64_t)t >= n) break;
+    if (threadIdx.x == 0) {
+      s_item[k ^ 1] = ahead;
+      ahead = atomicAdd(q, 1u);
+    }
     body((int64_t)t);
   }
 }
 
+// (seven blocks per SM for one- and two-byte voxels, as the tile pass alone)
 template <typename T, int CONN>
-__global__ void __launch_bounds__(kThreads, 6) k_batch_persistent(PersistentHeader* hdr) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) <= 2 ? 7 : 6) k_batch_persistent(PersistentHeader* hdr) {
   constexpr bool D3 = (CONN == 26 || CONN == 18 || CONN == 6);
   constexpr int TY = D3 ? 8 : 64, TZ = D3 ? 8 : 1;
   const LabelArgs& p = c_batch_args;

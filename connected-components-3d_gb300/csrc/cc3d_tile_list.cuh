@@ -764,9 +764,10 @@ __device__ __forceinline__ void tile_list_tile(const LabelArgs& p, const CUtenso
 
 // TMA: the box arrives by one TMA copy (else by plain loads); two kernels, so
 // that each holds only its own way of loading and keeps its registers for the
-// phases after it
+// phases after it.  Seven blocks per SM where the shared memory of one-
+// and two-byte boxes allows (40 registers a thread at six)
 template <typename T, int CONN, int TY, int TZ, int MODE, bool TMA>
-__global__ void __launch_bounds__(kThreads, 6)
+__global__ void __launch_bounds__(kThreads, sizeof(T) <= 2 ? 7 : 6)
 k_tile_list(LabelArgs p, const __grid_constant__ CUtensorMap tmap) {
   tile_list_tile<T, CONN, TY, TZ, MODE>(p, &tmap, TMA ? 1 : 0, p.tile_base + blockIdx.x);
 }
