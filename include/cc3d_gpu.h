@@ -465,8 +465,9 @@ int cc3d_gpu_label_batch(const cc3d_gpu_volume* volumes, int n, int dtype, int64
                          cc3d_gpu_volume_result* results, void* stream);
 /* How this thread's cc3d_gpu_label_batch runs (returns the previous mode):
  *   CC3D_BATCH_PERSISTENT (the default): ONE cooperative kernel launch walks
- *     every stage over the whole batch (tile pass, edge merges, numbering
- *     scan, per-volume results, labels) with bounded grid barriers between
+ *     every stage over the whole batch (tile pass, its blocks taking tiles
+ *     from a device work queue; edge merges, numbering scan, per-volume
+ *     results, labels) with bounded grid barriers between
  *     stages; its arguments come from a header uploaded to device memory, so
  *     the launch is captured into a CUDA graph once (per kernel, grid and
  *     workspace) and replayed for batches of any layout.  3D volumes use the
