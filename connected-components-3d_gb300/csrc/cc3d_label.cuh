@@ -659,6 +659,9 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
   const int64_t xg = x0 + g4;
   const bool vec = ((p.sx & 3) == 0) && ((reinterpret_cast<uintptr_t>(out) & (4 * sizeof(OUT) - 1)) == 0) &&
                    (sizeof(OUT) <= 4 || (reinterpret_cast<uintptr_t>(out) & 15) == 0);
+  const bool vec4 = vec && xg + 3 < p.sx;  // this lane's four voxels by one store
+  // a tile whose rows all lie inside the volume checks no row
+  const bool inner = y0 + TY <= p.sy && z0 + TZ <= p.sz;
   const int64_t plane = p.sx * p.sy;
   OUT* base_ptr = out + z0 * plane + y0 * p.sx + xg;
 #pragma unroll 2
@@ -667,23 +670,24 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
     const uint32_t F = __shfl_sync(FULL, r0 < 32 ? ma.x : mb.x, ri & 31);
     const uint32_t S = __shfl_sync(FULL, r0 < 32 ? ma.y : mb.y, ri & 31);
     const uint32_t b = __shfl_sync(FULL, r0 < 32 ? ra : rb, ri & 31);
+    // the row's records hold together (no foreground before its first run
+    // start, all its runs below C), checked once per row: then every
+    // foreground voxel's run index is in range
+    const bool ok = (F & ((S & (0u - S)) - 1u)) == 0u && b + (uint32_t)__popc(S) <= C;
+    if (!ok) atomicOr(&p.ctr->err, ERR_INDEX);
     OUT v[4];
     // run of voxel g4 (the last run start at or before it), then of the next three
-    int k = __popc(S & lanemask_le(g4)) - 1;
+    uint32_t r = b + (uint32_t)__popc(S & lanemask_le(g4)) - 1u;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      if (i) k += (S >> (g4 + i)) & 1u;
+      if (i) r += (S >> (g4 + i)) & 1u;
       v[i] = OUT(0);
-      if ((F >> (g4 + i)) & 1u) {
-        const uint32_t r = b + (uint32_t)k;
-        if (k >= 0 && r < C) v[i] = (OUT)(fast ? lab[r] : glab[r]);
-        else atomicOr(&p.ctr->err, ERR_INDEX);
-      }
+      if (ok && ((F >> (g4 + i)) & 1u)) v[i] = (OUT)(fast ? lab[r] : glab[r]);
     }
     const int ly = ri % TY, lz = ri / TY;
-    if (y0 + ly >= p.sy || z0 + lz >= p.sz) continue;
+    if (!inner && (y0 + ly >= p.sy || z0 + lz >= p.sz)) continue;
     OUT* dst = base_ptr + lz * plane + ly * p.sx;
-    if (vec && xg + 3 < p.sx) {
+    if (vec4) {
       if constexpr (sizeof(OUT) == 2) {
         *reinterpret_cast<uint2*>(dst) = make_uint2((uint32_t)v[0] | ((uint32_t)v[1] << 16),
                                                     (uint32_t)v[2] | ((uint32_t)v[3] << 16));

@@ -281,7 +281,8 @@ __device__ __forceinline__ void write_tile_warp(const LabelArgs& p, int64_t tile
   const uint32_t ra = p.rrow[tile * kRowsPerTile + lane], rb = p.rrow[tile * kRowsPerTile + 32 + lane];
   const int g4 = (lane & 7) * 4, rq = lane >> 3;
   const int64_t sx = v.sx, sy = v.sy, sz = v.sz, xg = x0 + g4, plane = sx * sy;
-  const bool vec = (sx & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & (4 * sizeof(OUT) - 1)) == 0;
+  const bool vec4 = (sx & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & (4 * sizeof(OUT) - 1)) == 0 && xg + 3 < sx;
+  const bool inner = y0 + TY <= sy && z0 + TZ <= sz;  // no row of the tile to check
   OUT* const base_ptr = out + z0 * plane + y0 * sx + xg;
 #pragma unroll 1
   for (int r0 = 0; r0 < kRowsPerTile; r0 += 4) {
@@ -289,23 +290,23 @@ __device__ __forceinline__ void write_tile_warp(const LabelArgs& p, int64_t tile
     const uint32_t F = __shfl_sync(FULL, r0 < 32 ? ma.x : mb.x, ri & 31);
     const uint32_t S = __shfl_sync(FULL, r0 < 32 ? ma.y : mb.y, ri & 31);
     const uint32_t b = __shfl_sync(FULL, r0 < 32 ? ra : rb, ri & 31);
+    // the row's records hold together (no foreground before its first run
+    // start, all its runs below C), checked once per row
+    const bool ok = (F & ((S & (0u - S)) - 1u)) == 0u && b + (uint32_t)__popc(S) <= C;
+    if (!ok) atomicOr(&p.ctr->err, ERR_INDEX);
     OUT o[4];
     // run of voxel g4 (the last run start at or before it), then of the next three
-    int k = __popc(S & lanemask_le(g4)) - 1;
+    uint32_t r = b + (uint32_t)__popc(S & lanemask_le(g4)) - 1u;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      if (i) k += (S >> (g4 + i)) & 1u;
+      if (i) r += (S >> (g4 + i)) & 1u;
       o[i] = OUT(0);
-      if ((F >> (g4 + i)) & 1u) {
-        const uint32_t r = b + (uint32_t)k;
-        if (k >= 0 && r < C) o[i] = (OUT)lab[r];
-        else atomicOr(&p.ctr->err, ERR_INDEX);
-      }
+      if (ok && ((F >> (g4 + i)) & 1u)) o[i] = (OUT)lab[r];
     }
     const int ly = ri % TY, lz = ri / TY;
-    if (y0 + ly >= sy || z0 + lz >= sz) continue;
+    if (!inner && (y0 + ly >= sy || z0 + lz >= sz)) continue;
     OUT* dst = base_ptr + lz * plane + ly * sx;
-    if (vec && xg + 3 < sx) {
+    if (vec4) {
       if constexpr (sizeof(OUT) == 2)
         *reinterpret_cast<uint2*>(dst) =
             make_uint2((uint32_t)o[0] | ((uint32_t)o[1] << 16), (uint32_t)o[2] | ((uint32_t)o[3] << 16));
