@@ -65,18 +65,6 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* bsum, int6
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------- resolve
-// one warp per tile (resolve_tile)
-__global__ void __launch_bounds__(256) k_resolve(LabelArgs p, int64_t ntiles) {
-  const int64_t tile = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (tile >= ntiles) return;
-  resolve_tile(p, tile, threadIdx.x & 31);
-}
-
-static void launch_resolve_all(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  if (ntiles > 0) k_resolve<<<(unsigned)((ntiles + 7) / 8), 256, 0, s>>>(a, ntiles);
-}
-
 // ---------------------------------------------------------------- writer
 template <typename OUT>
 cudaError_t launch_write_tiles_t(const LabelArgs& a, OUT* out, int64_t count, cudaStream_t s);
@@ -101,18 +89,29 @@ cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
-  launch_resolve_all(a, ntiles, s);
-  if (a.ty == 8 && a.tz == 8) k_write_batch<8, 8><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
-  else if (a.ty == 4 && a.tz == 16) k_write_batch<4, 16><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
-  else if (a.ty == 16 && a.tz == 4) k_write_batch<16, 4><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
-  else if (a.ty == 64 && a.tz == 1) k_write_batch<64, 1><<<(unsigned)ntiles, kThreads, 0, s>>>(a);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
+// A batch's labels, one warp per tile: the tile's run labels (resolve_tile),
+// then its rows in the volume's output type (write_tile_warp; a batch's
+// outputs are uint16 or uint32)
+template <int TY, int TZ>
+__global__ void __launch_bounds__(256) k_label_batch(LabelArgs p, int64_t ntiles) {
+  const int64_t tile = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (tile >= ntiles) return;
+  const int lane = threadIdx.x & 31;
+  resolve_tile(p, tile, lane);
+  __syncwarp();
+  const VolGeo& v = p.vols[p.tile_vol[tile]];
+  if (v.out_code == 2) write_tile_warp<uint16_t, TY, TZ>(p, tile, v, static_cast<uint16_t*>(v.out), lane);
+  else write_tile_warp<uint32_t, TY, TZ>(p, tile, v, static_cast<uint32_t*>(v.out), lane);
 }
 
-cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s) {
-  launch_resolve_all(a, a.ntiles, s);
+cudaError_t launch_write_batch(const LabelArgs& a, int64_t ntiles, cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((ntiles + 7) / 8);
+  if (a.ty == 8 && a.tz == 8) k_label_batch<8, 8><<<grid, 256, 0, s>>>(a, ntiles);
+  else if (a.ty == 4 && a.tz == 16) k_label_batch<4, 16><<<grid, 256, 0, s>>>(a, ntiles);
+  else if (a.ty == 16 && a.tz == 4) k_label_batch<16, 4><<<grid, 256, 0, s>>>(a, ntiles);
+  else if (a.ty == 64 && a.tz == 1) k_label_batch<64, 1><<<grid, 256, 0, s>>>(a, ntiles);
+  else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

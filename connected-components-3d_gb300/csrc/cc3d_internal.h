@@ -118,7 +118,6 @@ cudaError_t launch_scan(const LabelArgs& a, int64_t nwords, uint32_t* block_sums
 int64_t scan_blocks_needed(int64_t nwords);
 cudaError_t launch_write(const LabelArgs& a, void* out, int out_dtype, int64_t ntiles,
                          cudaStream_t s);
-cudaError_t launch_resolve(const LabelArgs& a, cudaStream_t s);
 cudaError_t launch_write_tiles(const LabelArgs& a, void* out, int out_dtype, int64_t count, cudaStream_t s);
 cudaError_t launch_batch_finalize(const LabelArgs& a, int nvol, int64_t nwords, BatchResult* res,
                                   cudaStream_t s);

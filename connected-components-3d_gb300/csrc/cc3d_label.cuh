@@ -37,8 +37,9 @@
 //   k_wrap_pairs  periodic boundaries: unions across wrapped faces.
 //   scan          exclusive popcount prefix of the bitmap: the rank of every
 //                 surviving key = the component's number minus one.
-//   k_resolve     label of each run = 1 + rank(key of its component's root)
-//   k_write       the run-length records expand to the output volume.
+//   k_label_write label of each run = 1 + rank(key of its component's root),
+//                 then the run-length records expand to the output volume
+//                 (batches: resolve_tile + write_tile_warp, cc3d_stages.cuh).
 //
 // Every loop that waits on other threads (the union-find retries) carries an
 // iteration budget; when it runs out it sets a bit in the device error word
@@ -506,65 +507,6 @@ __global__ void k_wrap_pairs(LabelArgs p, int conn) {
 }
 
 // -------------------------------------------------------------- K3: write
-// one CTA expands one tile's run records into its volume's output
-template <typename OUT, int TY, int TZ>
-__device__ __forceinline__ void write_tile(const LabelArgs& p, int64_t tile, OUT* out) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const TileGeo g = tile_geo(p, tile);
-  const int64_t x0 = (int64_t)g.tx * kTX, y0 = (int64_t)g.ty * TY, z0 = (int64_t)g.tz * TZ;
-  uint32_t C = p.tinfo[tile].C;
-  if (C > kTV) {
-    atomicOr(&p.ctr->err, ERR_INDEX);
-    C = kTV;
-  }
-  // final labels of the tile's runs, resolved by k_resolve.  Each warp owns
-  // 8 rows: the loads of all of them are issued before any store, so a warp
-  // waits for two rounds of loads (run masks and bases, run labels), not two
-  // per row.
-  constexpr int RPW = TY * TZ / (kThreads / 32);
-  static_assert(RPW * (kThreads / 32) == TY * TZ, "rows per warp");
-  const uint32_t* lab = p.label + tile * kTV;
-  const int64_t x = x0 + lane;
-  const bool xin = x < g.sx;
-  uint2 m[RPW];
-  int run[RPW];
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    const int ri = warp + j * (kThreads / 32);
-    m[j] = __ldg(p.rmask + tile * kRowsPerTile + ri);
-    run[j] = (int)__ldg(p.rrow + tile * kRowsPerTile + ri);
-  }
-  uint32_t c[RPW];  // run of every voxel
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    c[j] = 0xFFFFFFFFu;
-    if ((m[j].x >> lane) & 1u) {
-      const int k = __popc(m[j].y & lanemask_le(lane)) - 1;
-      c[j] = k >= 0 ? (uint32_t)(run[j] + k) : 0xFFFFFFFEu;
-    }
-  }
-  OUT v[RPW];
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    v[j] = OUT(0);
-    if (c[j] < C) v[j] = (OUT)__ldg(lab + c[j]);
-    else if (c[j] != 0xFFFFFFFFu) atomicOr(&p.ctr->err, ERR_INDEX);
-  }
-#pragma unroll
-  for (int j = 0; j < RPW; ++j) {
-    const int ri = warp + j * (kThreads / 32);
-    const int ly = ri % TY, lz = ri / TY;
-    const int64_t y = y0 + ly, z = z0 + lz;
-    if (xin && y < g.sy && z < g.sz) out[(z * g.sy + y) * g.sx + x] = v[j];
-  }
-}
-
-template <typename OUT, int TY, int TZ>
-__global__ void __launch_bounds__(kThreads)
-k_write(LabelArgs p, OUT* out) {
-  write_tile<OUT, TY, TZ>(p, p.tile_base + blockIdx.x, out);
-}
-
 // Label resolution and label writing of a single volume, one warp per tile:
 // the labels of the tile's root runs (1 + rank of their root's key among the
 // surviving keys), then every run's label (a non-root run copies its root
@@ -703,17 +645,6 @@ k_label_write(LabelArgs p, OUT* out, int64_t count) {
         if (xg + i < p.sx) dst[i] = v[i];
     }
   }
-}
-
-// a batch: every volume has its own output buffer and element type
-template <int TY, int TZ>
-__global__ void __launch_bounds__(kThreads)
-k_write_batch(LabelArgs p) {
-  const int64_t tile = p.tile_base + blockIdx.x;
-  const VolGeo& v = p.vols[p.tile_vol[tile]];
-  if (v.out_code == 2) write_tile<uint16_t, TY, TZ>(p, tile, static_cast<uint16_t*>(v.out));
-  else if (v.out_code == 3) write_tile<uint32_t, TY, TZ>(p, tile, static_cast<uint32_t*>(v.out));
-  else write_tile<uint64_t, TY, TZ>(p, tile, static_cast<uint64_t*>(v.out));
 }
 
 }  // namespace cc3dgpu
